@@ -1,0 +1,490 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 LBVH / traversal / transmittance path.
+
+Headline workload (one step): 256 independent random-triangle scenes with
+triangle counts log-uniform in [1e3, 1e6] (about 37 M triangles), 64 rays per
+triangle (about 2.4 G rays), built by one segmented LBVH build and traced by
+one persistent closest-hit launch.  Metric: aggregate Mrays/s of the step
+(build + trace), with the build time reported beside it, the plain
+one-scene-per-launch path measured on the same inputs, and the volume
+transmittance forward/adjoint pass on a 256^3 grid with 4,194,304 rays.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  All inputs are seeded synthetic data
+generated on the device (Philox streams); inputs exceed the 129 MB L2, so no
+flush is needed between steps.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s & LBVH ms, batched+adjoint vs plain on 1 GB300, t rel err ≤1e-5"
+N_SCENES = 256
+RAYS_PER_TRI = 64
+SEED_C0, SEED_C2, SEED_C3 = 0xF1ED0000, 0xF1ED0002, 0xF1ED0003
+# Algorithmic bytes (compulsory DRAM traffic): per ray 6 floats in + prim, t,
+# u, v out; per triangle of a batched build: bounds 36 + Morton 44 + sort
+# (histogram 4 + 5 passes x 24 counting the scene pass) + Karras 20 + refit 100.
+BYTES_PER_RAY = 24 + 16
+BYTES_PER_TRI_BATCHED = 36 + 44 + (4 + 5 * 24) + 20 + 100
+
+
+def scene_counts(seed: int = SEED_C3, n: int = N_SCENES) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    return np.round(np.exp(rng.uniform(math.log(1e3), math.log(1e6), n))).astype(np.int64)
+
+
+def peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={device}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows if len(r) >= 9 for k in range(4) if "Active" in r[5 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU reference arm (the oracle restates the reference; run on all host cores)
+# ---------------------------------------------------------------------------
+
+def cpu_sample(max_tris: int = 1_500_000, rays_cap: int = 2_000_000):
+    """Bounded sample of the headline workload for the CPU: the first scenes
+    of the batch up to max_tris triangles, 64 rays per triangle capped at
+    rays_cap rays, generated with numpy (same distributions)."""
+    counts = scene_counts()
+    keep, tot = [], 0
+    for c in counts:
+        if tot + c > max_tris:
+            break
+        keep.append(int(c))
+        tot += int(c)
+    rng = np.random.default_rng(7)
+    scenes = []
+    rays_left = rays_cap
+    for c in keep:
+        cent = rng.random((c, 1, 3), dtype=np.float32)
+        pos = (cent + (2 * rng.random((c, 3, 3), dtype=np.float32) - 1) * np.float32(0.01)).reshape(-1, 3)
+        nr = min(c * RAYS_PER_TRI, max(rays_left, 0))
+        rays_left -= nr
+        u = rng.random((nr, 5))
+        z = 1 - 2 * u[:, 0]
+        ph = 2 * np.pi * u[:, 1]
+        s = np.sqrt(np.maximum(0, 1 - z * z))
+        o = np.stack([0.5 + 2 * s * np.cos(ph), 0.5 + 2 * s * np.sin(ph), 0.5 + 2 * z])
+        d = u[:, 2:5].T - o
+        d /= np.linalg.norm(d, axis=0, keepdims=True)
+        r8 = np.zeros((8, nr), np.float32)
+        r8[0:3], r8[3:6], r8[6], r8[7] = o, d, 1e-4, np.inf
+        scenes.append((pos.astype(np.float32), r8))
+    return scenes
+
+
+def cpu_step(O, scenes):
+    t0 = time.perf_counter()
+    n_rays = 0
+    for pos, r8 in scenes:
+        n = pos.shape[0] // 3
+        tree = O.build_timed(pos, None, n)
+        tree["n"] = n
+        if r8.shape[1]:
+            O.trace_closest(pos, None, tree, r8, O.MODE_REF)
+        n_rays += r8.shape[1]
+    return n_rays, time.perf_counter() - t0
+
+
+def run_reference(args, rank: int) -> None:
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    scenes = cpu_sample()
+    for _ in range(max(args.warmup, 0) and 1):
+        cpu_step(O, scenes[:2])
+    rates = []
+    for _ in range(args.steps):
+        nr, dt = cpu_step(O, scenes)
+        rates.append(nr / dt / 1e6)
+    v = statistics.median(rates)
+    ntri = sum(p.shape[0] // 3 for p, _ in scenes)
+    nrays = sum(r.shape[1] for _, r in scenes)
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "Mrays/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(nrays / v / 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded numpy, same distributions as the GPU workload)",
+            "config": {"workload": "batched random-triangle scenes (config 3 generator), CPU sample",
+                       "scenes": len(scenes), "triangles": ntri, "rays": nrays},
+            "cpu_baseline": {"value": round(v, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                             "sample": f"{len(scenes)} scenes / {ntri} triangles / {nrays} rays per step: "
+                                       "oracle build (parallel bounds, Morton, 32-byte-record sort, Karras, "
+                                       "atomic refit) + recursive closest hit"},
+            "e2e": {"value": round(v, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_ours(args, rank: int, world: int, local_rank: int) -> None:
+    import torch
+    import fledge_gb300 as F
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+
+    def barrier():
+        if dist:
+            tdist.barrier()
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = F.Context(local_rank)
+    lib = ctx.lib
+    launches0 = lib.flg_ctx_launch_count(ctx.h)
+
+    # ---- inputs (device-resident, generated by Philox) ----
+    counts = scene_counts()
+    offs = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    roffs = offs * RAYS_PER_TRI
+    n_tri, n_rays = int(offs[-1]), int(roffs[-1])
+    pos = F.gen_triangles(ctx, n_tri, SEED_C3)
+    soa = torch.empty((6, n_rays), dtype=torch.float32, device=dev)
+    chunk = 1 << 28
+    for c0 in range(0, n_rays, chunk):
+        m = min(chunk, n_rays - c0)
+        ps = [C.c_void_p(soa[k, c0:].data_ptr()) for k in range(6)]
+        cen = (C.c_float * 3)(0.5, 0.5, 0.5)
+        ctx.check(lib.flg_gen_rays(ctx.h, SEED_C3 + 1, c0, m, cen, 2.0, *ps))
+    rays = F.Rays.from_soa(soa, tmin=1e-4)
+    hits = {"prim": torch.empty(n_rays, dtype=torch.int32, device=dev),
+            "t": torch.empty(n_rays, dtype=torch.float32, device=dev),
+            "u": torch.empty(n_rays, dtype=torch.float32, device=dev),
+            "v": torch.empty(n_rays, dtype=torch.float32, device=dev)}
+    mesh = F.InternalTriangleMesh(pos)
+    width, leaf = args.width, args.leaf
+    bb = F.BatchedRadixBVHBuilder(mesh, offs, ctx, node_width=width, leaf_size=leaf)
+    bb.build()
+    topts = dict(persistent=1, refill_lanes=args.refill, stack_depth=64)
+    ctx.sync()
+
+    stream = torch.cuda.current_stream(dev)
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        bb.build()
+        if ev:
+            ev[1].record(stream)
+        bb.intersect_batched(rays, roffs, out=hits, **topts)
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.sync()
+    barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler(local_rank)
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    l0 = lib.flg_ctx_launch_count(ctx.h)
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(evs[k])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    launches = lib.flg_ctx_launch_count(ctx.h) - l0
+    ctx.sync()
+    total_ms = t_start.elapsed_time(t_end)
+    build_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    trace_ms = [e[1].elapsed_time(e[2]) for e in evs]
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = world * n_rays / (ms_step * 1e-3) / 1e6
+    hit_rate = float((hits["prim"] >= 0).float().mean().item())
+
+    pk = peaks()
+    trace_bytes = n_rays * BYTES_PER_RAY + int(bb.info().device_bytes)
+    tr_ms = statistics.median(trace_ms)
+    roof = {"bound": "hbm", "achieved": round(trace_bytes / (tr_ms * 1e-3) / 1e9, 1), "peak": pk["hbm_gbs"],
+            "unit": "GB/s", "frac": None, "traffic": None, "kernel": "k_trace_persistent<4,false,64>",
+            "peak_source": pk["source"]}
+    roof["frac"] = round(roof["achieved"] / roof["peak"], 4)
+    b_ms = statistics.median(build_ms)
+    build_roof = {"achieved": round(n_tri * BYTES_PER_TRI_BATCHED / (b_ms * 1e-3) / 1e9, 1),
+                  "frac": round(n_tri * BYTES_PER_TRI_BATCHED / (b_ms * 1e-3) / 1e9 / pk["hbm_gbs"], 4),
+                  "bytes_per_tri": BYTES_PER_TRI_BATCHED}
+
+    # ---- plain path: one build + one trace launch per scene (BVH2 kernel) ----
+    plain = None
+    if not args.skip_plain:
+        handles = []
+        for s in range(N_SCENES):
+            sub = F.InternalTriangleMesh(pos[3 * offs[s]:3 * offs[s + 1]])
+            h = F.RadixBVHBuilder(sub, ctx, node_width=2)
+            h.build()
+            handles.append(h)
+        sub_rays = [F.Rays(*[soa[k, roffs[s]:roffs[s + 1]] for k in range(6)], tmin_const=1e-4)
+                    for s in range(N_SCENES)]
+        sub_hits = [{k: v[roffs[s]:roffs[s + 1]] for k, v in hits.items()} for s in range(N_SCENES)]
+
+        def plain_step():
+            for s in range(N_SCENES):
+                handles[s].build()
+                handles[s].intersect(sub_rays[s], out=sub_hits[s])
+        plain_step()
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.plain_steps):
+            plain_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pms = e0.elapsed_time(e1) / args.plain_steps
+        plain = {"ms_per_step": round(pms, 3), "mrays_s": round(n_rays / (pms * 1e-3) / 1e6, 2),
+                 "speedup_batched_vs_plain": round(pms / ms_step, 3)}
+        for h in handles:
+            h.destroy()
+        del handles
+
+    # ---- e2e: host (pinned) inputs, copies inside the timed region ----
+    e2e = None
+    if not args.skip_e2e:
+        e2e = run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, leaf, topts, dev, world)
+
+    # ---- volume: config 2 forward + adjoint ----
+    vol = run_volume(ctx, torch, F, dev) if not args.skip_volume else None
+
+    # ---- CPU baseline (rank 0) ----
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        from oracle import oracle as O
+        O.build()
+        cores = os.cpu_count() or 1
+        O.set_threads(cores)
+        scenes = cpu_sample(max_tris=600_000, rays_cap=1_000_000)
+        nr, dt = cpu_step(O, scenes)
+        ntri = sum(p.shape[0] // 3 for p, _ in scenes)
+        cpu = {"value": round(nr / dt / 1e6, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
+               "sample": f"{len(scenes)} scenes, {ntri} triangles, {nr} rays: oracle build + closest hit "
+                         f"({dt:.1f} s)"}
+
+    total_launches = lib.flg_ctx_launch_count(ctx.h) - launches0
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded Philox on device)",
+                "config": {"workload": "config 3: 256 batched random-triangle scenes, log-uniform [1e3,1e6] "
+                                       "triangles, 64 rays/triangle; segmented LBVH build + persistent trace",
+                           "triangles": n_tri, "rays": n_rays, "node_width": width, "leaf_size": leaf,
+                           "refill_lanes": args.refill, "l2": "inputs larger than L2 (no flush)",
+                           "parallelism": f"replicas x{world}"},
+                "build_ms": round(b_ms, 3), "trace_ms": round(tr_ms, 3), "hit_rate": round(hit_rate, 4),
+                "build_roofline": build_roof, "roofline": roof, "plain": plain, "volume": vol,
+                "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches),
+                "gpu_launches_total": int(total_launches)}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, leaf, topts, dev, world):
+    """Same step through the public API with host buffers: H2D of triangles
+    and rays from pinned memory, build, trace, D2H of the hits, all timed.
+    Rays move in chunks of scenes on a copy stream, overlapped with tracing."""
+    need = n_tri * 36 + n_rays * (24 + 16)
+    avail = 0
+    with open("/proc/meminfo") as f:
+        for line in f:
+            if line.startswith("MemAvailable:"):
+                avail = int(line.split()[1]) * 1024
+    if need > 0.6 * avail:
+        return {"value": None, "unit": "Mrays/s", "skipped": f"needs {need / 1e9:.0f} GB pinned host memory, "
+                                                             f"{avail / 1e9:.0f} GB available"}
+    h_pos = torch.empty(pos.shape, dtype=torch.float32, pin_memory=True)
+    h_pos.copy_(pos)
+    h_rays = torch.empty(soa.shape, dtype=torch.float32, pin_memory=True)
+    h_rays.copy_(soa)
+    h_out = {k: torch.empty(n_rays, dtype=torch.int32 if k == "prim" else torch.float32, pin_memory=True)
+             for k in ("prim", "t", "u", "v")}
+    d_pos = torch.empty_like(pos)
+    d_rays = torch.empty_like(soa)
+    d_out = {k: torch.empty(n_rays, dtype=v.dtype, device=dev) for k, v in h_out.items()}
+    bb = F.BatchedRadixBVHBuilder(F.InternalTriangleMesh(d_pos), offs, ctx, node_width=width, leaf_size=leaf)
+    d_pos.copy_(h_pos)
+    bb.build()
+    main = torch.cuda.current_stream(dev)
+    copy = torch.cuda.Stream(dev)
+    # scene groups of about 256 M rays
+    groups, g0 = [], 0
+    for s in range(N_SCENES):
+        if roffs[s + 1] - roffs[g0] >= (1 << 28) or s == N_SCENES - 1:
+            groups.append((g0, s + 1))
+            g0 = s + 1
+
+    def e2e_step():
+        d_pos.copy_(h_pos, non_blocking=True)
+        bb.build()
+        evs = []
+        for (a, b) in groups:
+            r0, r1 = int(roffs[a]), int(roffs[b])
+            with torch.cuda.stream(copy):
+                d_rays[:, r0:r1].copy_(h_rays[:, r0:r1], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(copy)
+            main.wait_event(ev)
+            ro = np.zeros(N_SCENES + 1, np.int64)
+            ro[a + 1:b + 1] = roffs[a + 1:b + 1] - roffs[a]
+            ro[b + 1:] = ro[b]
+            sub_rays = F.Rays(*[d_rays[k, r0:r1] for k in range(6)], tmin_const=1e-4)
+            sub_out = {k: v[r0:r1] for k, v in d_out.items()}
+            bb.intersect_batched(sub_rays, ro, out=sub_out, **topts)
+            done = torch.cuda.Event()
+            done.record(main)
+            evs.append((done, r0, r1))
+        for done, r0, r1 in evs:
+            copy.wait_event(done)
+            with torch.cuda.stream(copy):
+                for k in h_out:
+                    h_out[k][r0:r1].copy_(d_out[k][r0:r1], non_blocking=True)
+        main.wait_stream(copy)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / args.steps
+    ok = bool(torch.equal(h_out["prim"][:1 << 20].to(dev), d_out["prim"][:1 << 20]))
+    bb.destroy()
+    return {"value": round(world * n_rays / dt / 1e6, 2), "unit": "Mrays/s",
+            "h2d_bytes_per_step": int(n_tri * 36 + n_rays * 24), "d2h_bytes_per_step": int(n_rays * 16),
+            "ms_per_step": round(dt * 1e3, 3), "host_readback_consistent": ok}
+
+
+def run_volume(ctx, torch, F, dev):
+    """Config 2: 256^3 value-noise grid in [0,4], 4,194,304 rays, ratio
+    tracking forward (with checkpoints) and adjoint."""
+    rho = F.gen_noise_grid(ctx, 256, SEED_C2)
+    vol = F.DenseGridVolume(rho, medium=F.Medium(0.8, 0.2, 0.3, 0.1, 0.0), ctx=ctx)
+    soa = F.gen_rays(ctx, 1 << 22, SEED_C2 + 1)
+    rays = F.Rays.from_soa(soa)
+    T, ck = vol.tr(rays, SEED_C2, checkpoint=True)
+    dL = torch.ones_like(T)
+    grad = torch.zeros_like(rho)
+    for _ in range(3):
+        vol.tr(rays, SEED_C2, checkpoint=True)
+        vol.tr_adjoint(rays, SEED_C2, dL, T, ck, grad)
+    s = torch.cuda.current_stream(dev)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+    reps = 10
+    torch.cuda.synchronize()
+    e[0].record(s)
+    for _ in range(reps):
+        vol.tr(rays, SEED_C2, checkpoint=True)
+    e[1].record(s)
+    for _ in range(reps):
+        grad.zero_()
+        vol.tr_adjoint(rays, SEED_C2, dL, T, ck, grad)
+    e[2].record(s)
+    for _ in range(reps):
+        vol.tr_adjoint(rays, SEED_C2, dL, T, None, grad)
+    e[3].record(s)
+    torch.cuda.synchronize()
+    fwd = e[0].elapsed_time(e[1]) / reps
+    adj = e[1].elapsed_time(e[2]) / reps
+    adj_replay = e[2].elapsed_time(e[3]) / reps
+    vol.destroy()
+    return {"workload": "config 2: 256^3 grid, 4,194,304 rays", "fwd_ms": round(fwd, 4),
+            "adj_ms": round(adj, 4), "adj_replay_ms": round(adj_replay, 4),
+            "adj_over_fwd": round(adj / fwd, 3), "fwd_mrays_s": round((1 << 22) / (fwd * 1e-3) / 1e6, 1)}
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=4)
+    ap.add_argument("--leaf", type=int, default=1)
+    ap.add_argument("--refill", type=int, default=16)
+    ap.add_argument("--plain-steps", type=int, default=1)
+    ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-volume", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,245 @@
+// collapse.cu — re-lays out a built Karras BVH2 as 4- or 8-wide nodes for
+// traversal.  Top-down, one launch per level: each queued BVH2 node becomes a
+// wide node whose children are found by repeatedly opening the child with
+// the largest surface area (Wald, Benthin, Boulos 2008 style collapsing).
+// A BVH2 subtree covers a contiguous run of sorted triangles, so any subtree
+// with at most leaf_size triangles becomes a leaf range [first, first+count).
+// The Karras topology itself (the parity object) is unchanged.
+#include <algorithm>
+#include <climits>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace flg {
+
+constexpr int kMaxLevels = 64;
+
+struct Cand {
+  int32_t ref;     // BVH2 ref (>=0 internal, <0 ~leaf position)
+  int32_t first;   // first sorted triangle of the subtree
+  int32_t count;   // triangles in the subtree
+  float lo[3], hi[3];
+};
+
+__device__ __forceinline__ float half_area(const Cand &c) {
+  float dx = c.hi[0] - c.lo[0], dy = c.hi[1] - c.lo[1], dz = c.hi[2] - c.lo[2];
+  return dx * dy + dy * dz + dz * dx;
+}
+
+__device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, const int32_t *__restrict__ range_j,
+                                            const int64_t *__restrict__ tri_off,
+                                            const int64_t *__restrict__ node_off, int32_t ref, Cand &c0,
+                                            Cand &c1) {
+  const Node2 nd = nodes2[ref];
+  int32_t r[2] = {nd.d.x, nd.d.y};
+  Cand *o[2] = {&c0, &c1};
+  const float lo[2][3] = {{nd.a.x, nd.a.z, nd.c.x}, {nd.b.x, nd.b.z, nd.c.z}};
+  const float hi[2][3] = {{nd.a.y, nd.a.w, nd.c.y}, {nd.b.y, nd.b.w, nd.c.w}};
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    Cand &c = *o[k];
+    c.ref = r[k];
+    for (int a = 0; a < 3; ++a) {
+      c.lo[a] = lo[k][a];
+      c.hi[a] = hi[k][a];
+    }
+    if (r[k] < 0) {
+      c.first = ~r[k];
+      c.count = 1;
+    } else {
+      const Node2 &cn = nodes2[r[k]];
+      int s = cn.d.w;
+      int li = (int)(r[k] - node_off[s]);
+      int j = range_j[r[k]];
+      c.first = (int32_t)tri_off[s] + min(li, j);
+      c.count = abs(li - j) + 1;
+    }
+  }
+}
+
+template <int W>
+__global__ void __launch_bounds__(128)
+    k_collapse_level(const Node2 *__restrict__ nodes2, const int32_t *__restrict__ range_j,
+                     const int64_t *__restrict__ tri_off, const int64_t *__restrict__ node_off, int leaf_size,
+                     const int2 *__restrict__ q_in, const int32_t *__restrict__ q_in_count, int2 *__restrict__ q_out,
+                     int32_t *q_out_count, int32_t *node_ctr, int64_t cap, NodeW<W> *__restrict__ wide,
+                     uint32_t *err) {
+  const int cnt = *q_in_count;
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < cnt; it += gridDim.x * blockDim.x) {
+    const int2 item = q_in[it];
+    Cand c[W];
+    int nc = 2;
+    child_cands(nodes2, range_j, tri_off, node_off, item.x, c[0], c[1]);
+    while (nc < W) {
+      int best = -1;
+      float ba = -1.0f;
+#pragma unroll
+      for (int k = 0; k < W; ++k) {
+        if (k < nc && c[k].ref >= 0 && c[k].count > leaf_size) {
+          float a = half_area(c[k]);
+          if (a > ba) {
+            ba = a;
+            best = k;
+          }
+        }
+      }
+      if (best < 0) break;
+      Cand a, b;
+      int32_t r = 0;
+#pragma unroll
+      for (int k = 0; k < W; ++k)
+        if (k == best) r = c[k].ref;
+      child_cands(nodes2, range_j, tri_off, node_off, r, a, b);
+#pragma unroll
+      for (int k = 0; k < W; ++k) {
+        if (k == best) c[k] = a;
+        if (k == nc) c[k] = b;
+      }
+      ++nc;
+    }
+    NodeW<W> out;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      if (k < nc) {
+        out.lox[k] = c[k].lo[0];
+        out.loy[k] = c[k].lo[1];
+        out.loz[k] = c[k].lo[2];
+        out.hix[k] = c[k].hi[0];
+        out.hiy[k] = c[k].hi[1];
+        out.hiz[k] = c[k].hi[2];
+        if (c[k].ref < 0 || c[k].count <= leaf_size) {
+          out.child[k] = ~((c[k].first << 3) | (c[k].count - 1));
+        } else {
+          int slot = atomicAdd(node_ctr, 1);
+          if (slot >= cap) {
+            atomicOr(err, kErrQueue);
+            out.child[k] = kEmptyChild;
+          } else {
+            int qi = atomicAdd(q_out_count, 1);
+            q_out[qi] = make_int2(c[k].ref, slot);
+            out.child[k] = slot;
+          }
+        }
+      } else {
+        const float inf = __int_as_float(0x7f800000);
+        out.lox[k] = out.loy[k] = out.loz[k] = inf;
+        out.hix[k] = out.hiy[k] = out.hiz[k] = inf;
+        out.child[k] = kEmptyChild;
+      }
+    }
+    wide[item.y] = out;
+  }
+}
+
+__global__ void k_collapse_check(const int32_t *last_count, uint32_t *err) {
+  if (*last_count > 0) atomicOr(err, kErrQueue);
+}
+
+int collapse_reserve(flg_ctx ctx, flg_bvh b) {
+  // Every wide node corresponds to a distinct BVH2 internal node.
+  const int64_t cap = b->n_nodes + 1;
+  const size_t rec = b->width == 4 ? sizeof(NodeW<4>) : sizeof(NodeW<8>);
+  int rc = FLG_OK;
+  if (b->d_wide) {
+    cudaFree(b->d_wide);
+    b->allocs.erase(std::find(b->allocs.begin(), b->allocs.end(), b->d_wide));
+    b->device_bytes -= (int64_t)(b->wide_cap * (b->wide_rec));
+    b->d_wide = nullptr;
+  }
+  uint8_t *w = nullptr;
+  rc = halloc(b, &w, rec * (size_t)cap);
+  if (rc) return rc;
+  b->d_wide = w;
+  b->wide_cap = cap;
+  b->wide_rec = (int64_t)rec;
+  if (!b->d_wide_root) {
+    if ((rc = halloc(b, &b->d_wide_root, b->n_scenes))) return rc;
+    if ((rc = halloc(b, &b->d_wide_ctr, 2 * (kMaxLevels + 2)))) return rc;
+    if ((rc = halloc(b, &b->d_queue[0], cap))) return rc;
+    if ((rc = halloc(b, &b->d_queue[1], cap))) return rc;
+    if ((rc = halloc(b, &b->d_queue_init, b->n_scenes))) return rc;
+    std::vector<int32_t> roots(b->n_scenes);
+    std::vector<int2> q;
+    for (int s = 0; s < b->n_scenes; ++s) {
+      int64_t c = b->tri_off_h[s + 1] - b->tri_off_h[s];
+      if (c >= 2) {
+        roots[s] = (int32_t)q.size();
+        q.push_back(make_int2((int)b->node_off_h[s], (int)q.size()));
+      } else if (c == 1) {
+        roots[s] = ~(int32_t)(b->tri_off_h[s] << 3);
+      } else {
+        roots[s] = kEmptyChild;
+      }
+    }
+    b->n_wide_roots = (int32_t)q.size();
+    // counters: [0] nodes, [1 + L] queue size of level L; a static copy of
+    // the initial values follows at [kMaxLevels + 2].
+    std::vector<int32_t> ctr(2 * (kMaxLevels + 2), 0);
+    ctr[0] = b->n_wide_roots;
+    ctr[1] = b->n_wide_roots;
+    ctr[kMaxLevels + 2] = b->n_wide_roots;
+    ctr[kMaxLevels + 3] = b->n_wide_roots;
+    cudaStream_t st = ctx->stream;
+    cudaError_t e = cudaMemcpyAsync(b->d_wide_root, roots.data(), sizeof(int32_t) * b->n_scenes,
+                                    cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !q.empty())
+      e = cudaMemcpyAsync(b->d_queue_init, q.data(), sizeof(int2) * q.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(b->d_wide_ctr, ctr.data(), sizeof(int32_t) * ctr.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "collapse upload");
+  }
+  return FLG_OK;
+}
+
+template <int W>
+static int collapse_levels(flg_ctx ctx, flg_bvh b) {
+  cudaStream_t st = ctx->stream;
+  NodeW<W> *wide = (NodeW<W> *)b->d_wide;
+  const unsigned grid = (unsigned)ctx->num_sms * 4;
+  for (int L = 0; L < kMaxLevels; ++L) {
+    k_collapse_level<W><<<grid, 128, 0, st>>>(b->d_nodes2, b->d_range_j, b->d_tri_off, b->d_node_off,
+                                              b->leaf_size, b->d_queue[L & 1], b->d_wide_ctr + 1 + L,
+                                              b->d_queue[(L + 1) & 1], b->d_wide_ctr + 2 + L, b->d_wide_ctr,
+                                              b->wide_cap, wide, ctx->d_err);
+    FLG_LAUNCH_CHECK(ctx, "k_collapse_level");
+  }
+  k_collapse_check<<<1, 1, 0, st>>>(b->d_wide_ctr + 1 + kMaxLevels, ctx->d_err);
+  FLG_LAUNCH_CHECK(ctx, "k_collapse_check");
+  return FLG_OK;
+}
+
+int collapse_enqueue(flg_ctx ctx, flg_bvh b, int width, int leaf_size) {
+  (void)leaf_size;
+  if (b->n_wide_roots == 0) return FLG_OK;
+  cudaStream_t st = ctx->stream;
+  FLG_CUDA(ctx, cudaMemcpyAsync(b->d_wide_ctr, b->d_wide_ctr + kMaxLevels + 2,
+                                sizeof(int32_t) * (kMaxLevels + 2), cudaMemcpyDeviceToDevice, st));
+  FLG_CUDA(ctx, cudaMemcpyAsync(b->d_queue[0], b->d_queue_init, sizeof(int2) * b->n_wide_roots,
+                                cudaMemcpyDeviceToDevice, st));
+  return width == 4 ? collapse_levels<4>(ctx, b) : collapse_levels<8>(ctx, b);
+}
+
+}  // namespace flg
+
+using namespace flg;
+
+FLG_API int flg_bvh_set_width(flg_ctx ctx, flg_bvh bvh, int32_t node_width, int32_t leaf_size) {
+  if (!ctx || !bvh) return FLG_ERR_ARG;
+  if (node_width != 2 && node_width != 4 && node_width != 8)
+    return set_error(ctx, FLG_ERR_ARG, "node_width must be 2, 4 or 8");
+  if (leaf_size < 1 || leaf_size > 8) return set_error(ctx, FLG_ERR_ARG, "leaf_size must be in [1, 8]");
+  if (node_width == bvh->width && leaf_size == bvh->leaf_size) return FLG_OK;
+  const int old_w = bvh->width;
+  bvh->width = node_width;
+  bvh->leaf_size = leaf_size;
+  if (node_width == 2) return FLG_OK;
+  if (ctx->capturing && (old_w != node_width || !bvh->d_wide))
+    return set_error(ctx, FLG_ERR_STATE, "re-layout allocates; not allowed during capture");
+  if (!bvh->d_wide || old_w != node_width) {
+    int rc = collapse_reserve(ctx, bvh);
+    if (rc) return rc;
+  }
+  return collapse_enqueue(ctx, bvh, node_width, leaf_size);
+}

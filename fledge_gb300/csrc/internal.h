@@ -1,0 +1,179 @@
+// internal.h — host-side definitions shared by the translation units of
+// libflg: context and handle layouts, node records, launch helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/flg.h"
+
+namespace flg {
+
+// BVH2 node: both children's boxes in the parent (one 64-byte fetch tests
+// both children).  Child refs: >= 0 internal node (global index); < 0 leaf,
+// ~ref = sorted triangle position.
+struct alignas(16) Node2 {
+  float4 a;  // c0.lo.x c0.hi.x c0.lo.y c0.hi.y
+  float4 b;  // c1.lo.x c1.hi.x c1.lo.y c1.hi.y
+  float4 c;  // c0.lo.z c0.hi.z c1.lo.z c1.hi.z
+  int4 d;    // child0, child1, parent (global, -1 root), scene
+};
+
+// Wide node of width W, structure of arrays inside the record.  Child refs:
+// >= 0 wide node index; < 0 leaf range ~(first << 3 | (count - 1)) over
+// sorted triangles; kEmptyChild = unused slot.
+constexpr int32_t kEmptyChild = 0x7FFFFFFF;
+template <int W>
+struct alignas(16) NodeW {
+  float lox[W], hix[W], loy[W], hiy[W], loz[W], hiz[W];
+  int32_t child[W];
+};
+static_assert(sizeof(NodeW<4>) == 112, "NodeW<4> layout");
+static_assert(sizeof(NodeW<8>) == 224, "NodeW<8> layout");
+
+// Sorted triangle record: v0.xyz + original (scene-local) id, v1, v2.
+struct alignas(16) TriRec {
+  float4 p0, p1, p2;
+};
+
+}  // namespace flg
+
+struct flg_ctx_t {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // host staging overlap
+  bool own_stream = false;
+  uint32_t *d_err = nullptr;   // device error word
+  uint32_t *h_err = nullptr;   // pinned mirror
+  uint32_t spin_limit = 1u << 24;
+  bool capturing = false;
+  int num_sms = 0;
+  int64_t launches = 0;  // kernels launched through this context
+  std::string last_error;
+  // Traversal scratch: rays whose stack overflowed (retried with a deep
+  // stack), the persistent kernels' work counter, per-call ray offsets.
+  int64_t *d_ovf = nullptr;
+  uint32_t *d_ovf_count = nullptr;
+  int64_t ovf_cap = 0;
+  unsigned long long *d_work = nullptr;  // [0] persistent ray counter
+  int64_t *d_ray_off = nullptr;          // device copy of batched ray offsets
+  int64_t ray_off_cap = 0;
+  // Device staging buffers for flg_trace_closest_host (grown on demand).
+  void *stage = nullptr;
+  size_t stage_bytes = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+struct flg_bvh_t {
+  flg_ctx ctx = nullptr;
+  int64_t n_tri = 0, n_vert = 0, n_nodes = 0;
+  int32_t n_scenes = 0;
+  const float *pos = nullptr;
+  const int32_t *idx = nullptr;
+  std::vector<int64_t> tri_off_h, node_off_h;
+  int64_t *d_tri_off = nullptr, *d_node_off = nullptr;
+  int32_t *d_root = nullptr;     // per scene: root ref (node index, ~leaf, or INT32_MIN)
+  float *d_scene_box = nullptr;  // per scene: 6 floats (union of triangle boxes)
+  // Karras arrays.
+  uint32_t *d_keys = nullptr;    // sorted Morton codes (after build)
+  uint32_t *d_perm = nullptr;    // sorted position -> original global triangle
+  uint32_t *d_keys_alt = nullptr, *d_vals_alt = nullptr;
+  int32_t *d_split = nullptr;
+  uint8_t *d_leaf = nullptr;
+  int32_t *d_range_j = nullptr;
+  int32_t *d_parent = nullptr;
+  int32_t *d_leaf_parent = nullptr;
+  uint32_t *d_flags = nullptr;
+  flg::Node2 *d_nodes2 = nullptr;
+  flg::TriRec *d_tris = nullptr;
+  // Sort scratch.
+  uint32_t *d_hist = nullptr;      // [passes][256] counts, then exclusive offsets
+  uint32_t *d_lookback = nullptr;  // [passes][tiles][256]
+  uint32_t *d_tile_ctr = nullptr;  // [passes]
+  int32_t n_passes = 0, n_morton_passes = 0;
+  int64_t n_tiles = 0;
+  std::vector<uint32_t> scene_hist_h;  // scene-digit histograms (host)
+  // Wide layout.
+  int32_t width = 2, leaf_size = 1;
+  void *d_wide = nullptr;
+  int64_t wide_cap = 0, wide_rec = 0;
+  int32_t *d_wide_root = nullptr;  // per scene: wide root ref
+  int32_t *d_wide_ctr = nullptr;   // [0] nodes allocated, [1..] queue sizes
+  int2 *d_queue[2] = {nullptr, nullptr};
+  int2 *d_queue_init = nullptr;
+  int32_t n_wide_roots = 0;
+  std::vector<void *> allocs;
+  int64_t device_bytes = 0;
+  bool keep_topology = true;
+};
+
+struct flg_grid_t {
+  flg_ctx ctx = nullptr;
+  const float *rho = nullptr;
+  int32_t nx = 0, ny = 0, nz = 0;
+  float lo[3], hi[3], scale[3];
+  flg_medium medium{};
+  float sigma_t = 0.0f;
+  float *d_params = nullptr;  // [0] majorant, [1] 1/majorant
+};
+
+struct flg_graph_t {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace flg {
+
+int set_error(flg_ctx ctx, int code, const char *fmt, ...);
+int cuda_fail(flg_ctx ctx, cudaError_t e, const char *what);
+
+#define FLG_CUDA(ctx, call)                                   \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return ::flg::cuda_fail((ctx), e_, #call); \
+  } while (0)
+
+// Placed after every kernel launch: counts the launch on the context and
+// turns a launch error into a status.
+#define FLG_LAUNCH_CHECK(ctx, what)                                 \
+  do {                                                              \
+    ++(ctx)->launches;                                              \
+    cudaError_t e_ = cudaGetLastError();                            \
+    if (e_ != cudaSuccess) return ::flg::cuda_fail((ctx), e_, what); \
+  } while (0)
+
+// Device allocation owned by a handle.
+template <class T>
+int halloc(flg_bvh b, T **p, size_t count) {
+  size_t bytes = count * sizeof(T);
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc((void **)p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(b->ctx, FLG_ERR_OOM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  b->allocs.push_back((void *)*p);
+  b->device_bytes += (int64_t)bytes;
+  return FLG_OK;
+}
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Launch-size helper: grid of `n` items, capped at `cap_blocks`.
+inline unsigned grid_for(int64_t n, int threads, int64_t cap_blocks = 1 << 30) {
+  int64_t g = ceil_div(n > 0 ? n : 1, threads);
+  if (g > cap_blocks) g = cap_blocks;
+  return (unsigned)g;
+}
+
+// Defined in the build / trace translation units.
+int build_enqueue(flg_ctx ctx, flg_bvh b);
+int collapse_reserve(flg_ctx ctx, flg_bvh b);
+int collapse_enqueue(flg_ctx ctx, flg_bvh b, int width, int leaf_size);
+int sort_enqueue(flg_ctx ctx, flg_bvh b);
+
+}  // namespace flg

@@ -1,0 +1,726 @@
+// trace.cu — closest-hit and any-hit ray traversal (RadixBVHBuilder::
+// intersect / recursiveIntersect, radix_bvh.cpp:26-30,202-245, with the
+// watertight Pluecker test of intersector.hpp:63-101).
+//
+// Layouts: BVH2 nodes carry both children's boxes (one 64-byte record per
+// visit); wide nodes (4 or 8 children) store their child boxes as structure
+// of arrays inside a 112/224-byte record read with 16-byte loads; triangles
+// are gathered in sorted (leaf) order, 48 bytes each.
+//
+// Kernels:
+//   k_trace_bvh2        one ray per thread over BVH2, leaf triangles tested
+//                       directly as the reference does (no leaf box test)
+//   k_trace_wide        one ray per thread over 4/8-wide nodes, children
+//                       visited nearest first (sorting network on t|ref keys)
+//   k_trace_persistent  persistent warps that refill idle lanes from a global
+//                       ray counter (work stealing across scenes of a batch)
+//   k_trace_retry       rays whose short stack overflowed, with a deep stack
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace flg {
+
+struct RaySoA {
+  const float *ox, *oy, *oz, *dx, *dy, *dz, *tmin, *tmax;
+  float tmin_c, tmax_c;
+};
+
+struct Out {
+  int32_t *prim;
+  float *t, *u, *v;
+  uint8_t *occ;
+};
+
+struct Scratch {
+  int64_t *ovf;
+  uint32_t *ovf_count;
+  int64_t ovf_cap;
+  unsigned long long *work;
+  uint32_t *err;
+};
+
+constexpr int kRetryStack = 256;
+
+__device__ __forceinline__ void load_ray(const RaySoA &R, int64_t i, float3 &o, float3 &d, float3 &inv,
+                                         float &tmin, float &tmax) {
+  o = make_float3(__ldg(R.ox + i), __ldg(R.oy + i), __ldg(R.oz + i));
+  d = make_float3(__ldg(R.dx + i), __ldg(R.dy + i), __ldg(R.dz + i));
+  inv = make_float3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
+  tmin = R.tmin ? __ldg(R.tmin + i) : R.tmin_c;
+  tmax = R.tmax ? __ldg(R.tmax + i) : R.tmax_c;
+}
+
+__device__ __forceinline__ int32_t scene_root(const int32_t *__restrict__ roots, const int64_t *__restrict__ ray_off,
+                                              int n_scenes, int64_t i) {
+  int s = ray_off ? find_segment(ray_off, n_scenes, i) : 0;
+  return __ldg(roots + s);
+}
+
+// Tests sorted triangle g; updates the closest hit.  Returns true on accept.
+__device__ __forceinline__ bool test_tri(const TriRec *__restrict__ tris, int64_t g, const float3 &o,
+                                         const float3 &d, float tmin, float &best, bool &have, int32_t &prim,
+                                         float &hu, float &hv) {
+  const float4 *p = (const float4 *)(tris + g);
+  float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+  float t, u, v;
+  if (!pluecker(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z), o, d, t,
+                u, v))
+    return false;
+  if (!accept_closest(t, tmin, best, have)) return false;
+  best = t;
+  have = true;
+  prim = __float_as_int(a.w);
+  hu = u;
+  hv = v;
+  return true;
+}
+
+// Any-hit variant: accepts t in [tmin, tmax].
+__device__ __forceinline__ bool test_tri_any(const TriRec *__restrict__ tris, int64_t g, const float3 &o,
+                                             const float3 &d, float tmin, float tmax) {
+  const float4 *p = (const float4 *)(tris + g);
+  float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+  float t, u, v;
+  if (!pluecker(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z), o, d, t,
+                u, v))
+    return false;
+  return t >= tmin && !(t > tmax);
+}
+
+__device__ __forceinline__ uint64_t stack_key(float t, int32_t ref) {
+  return ((uint64_t)(__float_as_uint(t) & 0x7FFFFFFFu) << 32) | (uint32_t)ref;
+}
+
+__device__ __forceinline__ void write_result(const Out &O, int64_t i, bool any, bool have, int32_t prim,
+                                             float best, float tmax, float u, float v) {
+  if (any) {
+    O.occ[i] = have ? 1 : 0;
+  } else {
+    O.prim[i] = have ? prim : -1;
+    O.t[i] = have ? best : tmax;
+    O.u[i] = have ? u : 0.0f;
+    O.v[i] = have ? v : 0.0f;
+  }
+}
+
+__device__ __forceinline__ void record_overflow(const Scratch &S, int64_t ray) {
+  uint32_t k = atomicAdd(S.ovf_count, 1u);
+  if (k < S.ovf_cap) S.ovf[k] = ray;
+  else atomicOr(S.err, kErrStack);
+}
+
+// ----------------------------------------------------------------------------
+// BVH2 traversal (reference-faithful leaf handling).
+// ----------------------------------------------------------------------------
+template <bool ANY, int STACK>
+__device__ __forceinline__ bool trace_bvh2(const Node2 *__restrict__ nodes, const TriRec *__restrict__ tris,
+                                           int32_t root, const float3 &o, const float3 &d, const float3 &inv,
+                                           float tmin, float tmax, bool &have, int32_t &prim, float &best,
+                                           float &hu, float &hv) {
+  best = tmax;
+  have = false;
+  prim = -1;
+  hu = hv = 0.0f;
+  if (root == INT32_MIN) return true;
+  if (root < 0) {
+    if (ANY) have = test_tri_any(tris, ~(int64_t)root, o, d, tmin, tmax);
+    else test_tri(tris, ~(int64_t)root, o, d, tmin, best, have, prim, hu, hv);
+    return true;
+  }
+  uint64_t stk[STACK];
+  int sp = 0;
+  int32_t cur = root;
+  const float inf = __int_as_float(0x7f800000);
+  while (true) {
+    const float4 *np = (const float4 *)(nodes + cur);
+    const float4 A = __ldg(np), B = __ldg(np + 1), C = __ldg(np + 2);
+    const int4 Dd = __ldg((const int4 *)(np + 3));
+    const int32_t c0 = Dd.x, c1 = Dd.y;
+    if (c0 < 0) {
+      if (ANY) {
+        if (test_tri_any(tris, ~(int64_t)c0, o, d, tmin, tmax)) { have = true; return true; }
+      } else {
+        test_tri(tris, ~(int64_t)c0, o, d, tmin, best, have, prim, hu, hv);
+      }
+    }
+    if (c1 < 0) {
+      if (ANY) {
+        if (test_tri_any(tris, ~(int64_t)c1, o, d, tmin, tmax)) { have = true; return true; }
+      } else {
+        test_tri(tris, ~(int64_t)c1, o, d, tmin, best, have, prim, hu, hv);
+      }
+    }
+    const float lim = ANY ? tmax : best;
+    float t0 = c0 >= 0 ? slab_tnear(A.x, A.y, A.z, A.w, C.x, C.y, o, inv) : inf;
+    float t1 = c1 >= 0 ? slab_tnear(B.x, B.y, B.z, B.w, C.z, C.w, o, inv) : inf;
+    const bool h0 = t0 <= lim, h1 = t1 <= lim;
+    if (h0 && h1) {
+      if (sp >= STACK) return false;
+      const bool swap = t1 < t0;
+      stk[sp++] = swap ? stack_key(t0, c0) : stack_key(t1, c1);
+      cur = swap ? c1 : c0;
+      continue;
+    }
+    if (h0) { cur = c0; continue; }
+    if (h1) { cur = c1; continue; }
+    bool found = false;
+    while (sp > 0) {
+      uint64_t e = stk[--sp];
+      if (__uint_as_float((uint32_t)(e >> 32)) > (ANY ? tmax : best)) continue;
+      cur = (int32_t)(uint32_t)e;
+      found = true;
+      break;
+    }
+    if (!found) return true;
+  }
+}
+
+template <bool ANY>
+__global__ void __launch_bounds__(256)
+    k_trace_bvh2(const Node2 *__restrict__ nodes, const TriRec *__restrict__ tris, const int32_t *__restrict__ roots,
+                 const int64_t *__restrict__ ray_off, int n_scenes, RaySoA R, int64_t n, Out O, Scratch S) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float3 o, d, inv;
+  float tmin, tmax;
+  load_ray(R, i, o, d, inv, tmin, tmax);
+  const int32_t root = scene_root(roots, ray_off, n_scenes, i);
+  bool have;
+  int32_t prim;
+  float best, hu, hv;
+  if (!trace_bvh2<ANY, 64>(nodes, tris, root, o, d, inv, tmin, tmax, have, prim, best, hu, hv)) {
+    record_overflow(S, i);
+    return;
+  }
+  write_result(O, i, ANY, have, prim, best, tmax, hu, hv);
+}
+
+// ----------------------------------------------------------------------------
+// Wide traversal as a resumable state machine (one node or leaf range per
+// step) so the persistent kernel can swap rays between steps.
+// ----------------------------------------------------------------------------
+template <int W>
+__device__ __forceinline__ void cas(uint64_t &a, uint64_t &b) {
+  uint64_t lo = a < b ? a : b, hi = a < b ? b : a;
+  a = lo;
+  b = hi;
+}
+
+template <int W>
+__device__ __forceinline__ void sort_keys(uint64_t (&k)[W]) {
+  if constexpr (W == 4) {
+    cas<W>(k[0], k[1]); cas<W>(k[2], k[3]); cas<W>(k[0], k[2]); cas<W>(k[1], k[3]); cas<W>(k[1], k[2]);
+  } else {
+    cas<W>(k[0], k[1]); cas<W>(k[2], k[3]); cas<W>(k[4], k[5]); cas<W>(k[6], k[7]);
+    cas<W>(k[0], k[2]); cas<W>(k[1], k[3]); cas<W>(k[4], k[6]); cas<W>(k[5], k[7]);
+    cas<W>(k[1], k[2]); cas<W>(k[5], k[6]);
+    cas<W>(k[0], k[4]); cas<W>(k[1], k[5]); cas<W>(k[2], k[6]); cas<W>(k[3], k[7]);
+    cas<W>(k[2], k[4]); cas<W>(k[3], k[5]);
+    cas<W>(k[1], k[2]); cas<W>(k[3], k[4]); cas<W>(k[5], k[6]);
+  }
+}
+
+template <int W, bool ANY, int STACK>
+struct Tracer {
+  float3 o, d, inv;
+  float tmin, tmax, best, hu, hv;
+  int32_t cur, prim;
+  int sp;
+  bool have, overflow;
+  uint64_t stk[STACK];
+
+  __device__ __forceinline__ void start(int32_t root) {
+    best = tmax;
+    have = false;
+    overflow = false;
+    prim = -1;
+    hu = hv = 0.0f;
+    sp = 0;
+    cur = root;
+  }
+
+  __device__ __forceinline__ bool pop() {
+    const float lim = ANY ? tmax : best;
+    while (sp > 0) {
+      uint64_t e = stk[--sp];
+      if (__uint_as_float((uint32_t)(e >> 32)) > lim) continue;
+      cur = (int32_t)(uint32_t)e;
+      return true;
+    }
+    return false;
+  }
+
+  // Returns true when the ray is finished.
+  __device__ __forceinline__ bool step(const NodeW<W> *__restrict__ nodes, const TriRec *__restrict__ tris) {
+    if (cur == kEmptyChild || cur == INT32_MIN) return true;
+    if (cur >= 0) {
+      constexpr int NV = 7 * W / 4;  // float4 per record
+      float f[4 * NV];
+      const float4 *np = (const float4 *)(nodes + cur);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        float4 q = __ldg(np + k);
+        f[4 * k] = q.x; f[4 * k + 1] = q.y; f[4 * k + 2] = q.z; f[4 * k + 3] = q.w;
+      }
+      const float lim = ANY ? tmax : best;
+      uint64_t key[W];
+      int nh = 0;
+#pragma unroll
+      for (int k = 0; k < W; ++k) {
+        const int32_t ref = __float_as_int(f[6 * W + k]);
+        float t = slab_tnear(f[k], f[W + k], f[2 * W + k], f[3 * W + k], f[4 * W + k], f[5 * W + k], o, inv);
+        const bool ok = ref != kEmptyChild && t <= lim;
+        key[k] = ok ? stack_key(t, ref) : ~0ull;
+        nh += ok ? 1 : 0;
+      }
+      if (nh == 0) return !pop();
+      sort_keys<W>(key);
+      if (sp + nh - 1 > STACK) {
+        overflow = true;
+        return true;
+      }
+#pragma unroll
+      for (int k = W - 1; k >= 1; --k)
+        if (k < nh) stk[sp++] = key[k];
+      cur = (int32_t)(uint32_t)key[0];
+      return false;
+    }
+    const int32_t enc = ~cur;
+    const int64_t first = (int64_t)((uint32_t)enc >> 3);
+    const int count = (enc & 7) + 1;
+    for (int j = 0; j < count; ++j) {
+      if (ANY) {
+        if (test_tri_any(tris, first + j, o, d, tmin, tmax)) {
+          have = true;
+          return true;
+        }
+      } else {
+        test_tri(tris, first + j, o, d, tmin, best, have, prim, hu, hv);
+      }
+    }
+    return !pop();
+  }
+};
+
+template <int W, bool ANY, int STACK>
+__global__ void __launch_bounds__(256)
+    k_trace_wide(const NodeW<W> *__restrict__ nodes, const TriRec *__restrict__ tris, const int32_t *__restrict__ roots,
+                 const int64_t *__restrict__ ray_off, int n_scenes, RaySoA R, int64_t n, Out O, Scratch S) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Tracer<W, ANY, STACK> tr;
+  load_ray(R, i, tr.o, tr.d, tr.inv, tr.tmin, tr.tmax);
+  tr.start(scene_root(roots, ray_off, n_scenes, i));
+  while (!tr.step(nodes, tris)) {
+  }
+  if (tr.overflow) record_overflow(S, i);
+  else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv);
+}
+
+template <int W, bool ANY, int STACK>
+__global__ void __launch_bounds__(256)
+    k_trace_persistent(const NodeW<W> *__restrict__ nodes, const TriRec *__restrict__ tris,
+                       const int32_t *__restrict__ roots, const int64_t *__restrict__ ray_off, int n_scenes, RaySoA R,
+                       int64_t n, Out O, Scratch S, int refill) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt = (1u << lane) - 1u;
+  Tracer<W, ANY, STACK> tr;
+  bool active = false, exhausted = false;
+  int64_t ray = -1;
+  while (true) {
+    const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active);
+    const int nidle = __popc(idle);
+    if (!exhausted && nidle >= refill) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(S.work, (unsigned long long)nidle);
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (!active) {
+        const int64_t my = (int64_t)base + __popc(idle & lt);
+        if (my < n) {
+          ray = my;
+          load_ray(R, ray, tr.o, tr.d, tr.inv, tr.tmin, tr.tmax);
+          tr.start(scene_root(roots, ray_off, n_scenes, ray));
+          active = true;
+        }
+      }
+      if ((int64_t)base + nidle >= n) exhausted = true;
+    }
+    if (__ballot_sync(0xFFFFFFFFu, active) == 0u) {
+      if (exhausted) break;
+      continue;
+    }
+    if (active && tr.step(nodes, tris)) {
+      if (tr.overflow) record_overflow(S, ray);
+      else write_result(O, ray, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv);
+      active = false;
+    }
+  }
+}
+
+template <int W, bool ANY>
+__global__ void __launch_bounds__(128)
+    k_trace_retry(const NodeW<(W == 2 ? 4 : W)> *__restrict__ nodes, const Node2 *__restrict__ nodes2,
+                  const TriRec *__restrict__ tris,
+                  const int32_t *__restrict__ roots, const int64_t *__restrict__ ray_off, int n_scenes, RaySoA R, Out O,
+                  Scratch S) {
+  const uint32_t cnt = min((int64_t)*S.ovf_count, S.ovf_cap);
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += gridDim.x * blockDim.x) {
+    const int64_t i = S.ovf[j];
+    float3 o, d, inv;
+    float tmin, tmax;
+    load_ray(R, i, o, d, inv, tmin, tmax);
+    const int32_t root = scene_root(roots, ray_off, n_scenes, i);
+    if (W == 2) {
+      bool have;
+      int32_t prim;
+      float best, hu, hv;
+      if (!trace_bvh2<ANY, kRetryStack>(nodes2, tris, root, o, d, inv, tmin, tmax, have, prim, best, hu, hv)) {
+        atomicOr(S.err, kErrStack);
+        continue;
+      }
+      write_result(O, i, ANY, have, prim, best, tmax, hu, hv);
+    } else {
+      Tracer<(W == 2 ? 4 : W), ANY, kRetryStack> tr;
+      tr.o = o; tr.d = d; tr.inv = inv; tr.tmin = tmin; tr.tmax = tmax;
+      tr.start(root);
+      while (!tr.step(nodes, tris)) {
+      }
+      if (tr.overflow) atomicOr(S.err, kErrStack);
+      else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv);
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// Host side.
+// ----------------------------------------------------------------------------
+
+static int ensure_trace_scratch(flg_ctx ctx) {
+  if (ctx->d_ovf) return FLG_OK;
+  if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "first trace allocates; not allowed during capture");
+  ctx->ovf_cap = 1 << 20;
+  // Two sets (index 0: default stream, 1: staging second stream).
+  FLG_CUDA(ctx, cudaMalloc((void **)&ctx->d_ovf, sizeof(int64_t) * ctx->ovf_cap * 2));
+  FLG_CUDA(ctx, cudaMalloc((void **)&ctx->d_ovf_count, sizeof(uint32_t) * 2));
+  FLG_CUDA(ctx, cudaMalloc((void **)&ctx->d_work, sizeof(unsigned long long) * 2));
+  return FLG_OK;
+}
+
+static Scratch scratch_for(flg_ctx ctx, int set) {
+  return Scratch{ctx->d_ovf + set * ctx->ovf_cap, ctx->d_ovf_count + set, ctx->ovf_cap, ctx->d_work + set,
+                 ctx->d_err};
+}
+
+static int check_rays(flg_ctx ctx, const flg_rays *r, int64_t n) {
+  if (!r) return set_error(ctx, FLG_ERR_ARG, "rays is NULL");
+  if (n < 0) return set_error(ctx, FLG_ERR_ARG, "n < 0");
+  if (n > 0 && (!r->ox || !r->oy || !r->oz || !r->dx || !r->dy || !r->dz))
+    return set_error(ctx, FLG_ERR_ARG, "ray origin/direction pointer is NULL");
+  return FLG_OK;
+}
+
+template <int W, bool ANY>
+static void launch_wide(flg_ctx ctx, cudaStream_t st, flg_bvh b, const RaySoA &R, int64_t n, const Out &O,
+                        const Scratch &S, const int64_t *ray_off, int n_scenes, const flg_trace_opts &op) {
+  const NodeW<W> *nodes = (const NodeW<W> *)b->d_wide;
+  const int threads = op.block_threads;
+  if (op.persistent) {
+    int per_sm = 0;
+    if (op.stack_depth <= 32)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_persistent<W, ANY, 32>, threads, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_persistent<W, ANY, 64>, threads, 0);
+    if (per_sm < 1) per_sm = 1;
+    int64_t want = ceil_div(n, threads);
+    int64_t g = std::min<int64_t>((int64_t)per_sm * ctx->num_sms, want);
+    if (g < 1) g = 1;
+    const int refill = std::max(1, std::min(32, op.refill_lanes));
+    if (op.stack_depth <= 32)
+      k_trace_persistent<W, ANY, 32><<<(unsigned)g, threads, 0, st>>>(nodes, b->d_tris, b->d_wide_root, ray_off,
+                                                                      n_scenes, R, n, O, S, refill);
+    else
+      k_trace_persistent<W, ANY, 64><<<(unsigned)g, threads, 0, st>>>(nodes, b->d_tris, b->d_wide_root, ray_off,
+                                                                      n_scenes, R, n, O, S, refill);
+  } else {
+    const unsigned g = (unsigned)ceil_div(n, threads);
+    if (op.stack_depth <= 32)
+      k_trace_wide<W, ANY, 32><<<g, threads, 0, st>>>(nodes, b->d_tris, b->d_wide_root, ray_off, n_scenes, R, n, O,
+                                                      S);
+    else
+      k_trace_wide<W, ANY, 64><<<g, threads, 0, st>>>(nodes, b->d_tris, b->d_wide_root, ray_off, n_scenes, R, n, O,
+                                                      S);
+  }
+}
+
+// Enqueues one traversal of n rays on stream st with scratch set `set`.
+int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_rays *rays, int64_t n,
+                  const flg_trace_opts *opts, const int64_t *ray_off_dev, int n_scenes, flg_hits *hits,
+                  uint8_t *occ) {
+  flg_trace_opts op{};
+  if (opts) op = *opts;
+  if (op.stack_depth == 0) op.stack_depth = 64;
+  if (op.block_threads == 0) op.block_threads = 256;
+  if (op.refill_lanes == 0) op.refill_lanes = 16;
+  if (op.stack_depth != 32 && op.stack_depth != 64) return set_error(ctx, FLG_ERR_ARG, "stack_depth must be 32 or 64");
+  if (op.block_threads != 64 && op.block_threads != 128 && op.block_threads != 256)
+    return set_error(ctx, FLG_ERR_ARG, "block_threads must be 64, 128 or 256");
+  if (op.ray_sort) return set_error(ctx, FLG_ERR_UNSUPPORTED, "ray_sort is not implemented");
+  int rc = ensure_trace_scratch(ctx);
+  if (rc) return rc;
+  if (n == 0) return FLG_OK;
+  RaySoA R{rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmin, rays->tmax,
+           rays->tmin_const, rays->tmax_const};
+  Out O{hits ? hits->prim : nullptr, hits ? hits->t : nullptr, hits ? hits->u : nullptr,
+        hits ? hits->v : nullptr, occ};
+  Scratch S = scratch_for(ctx, set);
+  FLG_CUDA(ctx, cudaMemsetAsync(S.ovf_count, 0, sizeof(uint32_t), st));
+  FLG_CUDA(ctx, cudaMemsetAsync(S.work, 0, sizeof(unsigned long long), st));
+  const bool any = occ != nullptr;
+  if (b->width == 2) {
+    const unsigned g = (unsigned)ceil_div(n, 256);
+    if (any)
+      k_trace_bvh2<true><<<g, 256, 0, st>>>(b->d_nodes2, b->d_tris, b->d_root, ray_off_dev, n_scenes, R, n, O, S);
+    else
+      k_trace_bvh2<false><<<g, 256, 0, st>>>(b->d_nodes2, b->d_tris, b->d_root, ray_off_dev, n_scenes, R, n, O, S);
+  } else if (b->width == 4) {
+    if (any) launch_wide<4, true>(ctx, st, b, R, n, O, S, ray_off_dev, n_scenes, op);
+    else launch_wide<4, false>(ctx, st, b, R, n, O, S, ray_off_dev, n_scenes, op);
+  } else {
+    if (any) launch_wide<8, true>(ctx, st, b, R, n, O, S, ray_off_dev, n_scenes, op);
+    else launch_wide<8, false>(ctx, st, b, R, n, O, S, ray_off_dev, n_scenes, op);
+  }
+  FLG_LAUNCH_CHECK(ctx, "trace kernel");
+  const unsigned rg = (unsigned)ctx->num_sms;
+  const void *wide = b->d_wide;
+  const int32_t *roots = b->width == 2 ? b->d_root : b->d_wide_root;
+#define FLG_RETRY(WW)                                                                                       \
+  if (any)                                                                                                  \
+    k_trace_retry<WW, true><<<rg, 128, 0, st>>>((const NodeW<(WW == 2 ? 4 : WW)> *)wide, b->d_nodes2,       \
+                                                b->d_tris, roots, ray_off_dev, n_scenes, R, O, S);          \
+  else                                                                                                      \
+    k_trace_retry<WW, false><<<rg, 128, 0, st>>>((const NodeW<(WW == 2 ? 4 : WW)> *)wide, b->d_nodes2,      \
+                                                 b->d_tris, roots, ray_off_dev, n_scenes, R, O, S);
+  if (b->width == 2) {
+    FLG_RETRY(2)
+  } else if (b->width == 4) {
+    FLG_RETRY(4)
+  } else {
+    FLG_RETRY(8)
+  }
+#undef FLG_RETRY
+  FLG_LAUNCH_CHECK(ctx, "trace retry kernel");
+  return FLG_OK;
+}
+
+}  // namespace flg
+
+using namespace flg;
+
+FLG_API int flg_trace_closest(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n,
+                              const flg_trace_opts *opts, flg_hits *out) {
+  if (!ctx || !bvh || !out) return ctx ? set_error(ctx, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
+  int rc = check_rays(ctx, rays, n);
+  if (rc) return rc;
+  if (n > 0 && (!out->prim || !out->t || !out->u || !out->v))
+    return set_error(ctx, FLG_ERR_ARG, "hit output pointer is NULL");
+  if (bvh->n_scenes != 1) return set_error(ctx, FLG_ERR_ARG, "batched handle: use flg_trace_closest_batched");
+  return trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, opts, nullptr, 1, out, nullptr);
+}
+
+FLG_API int flg_trace_any(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n, const flg_trace_opts *opts,
+                          uint8_t *occluded) {
+  if (!ctx || !bvh) return ctx ? set_error(ctx, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
+  int rc = check_rays(ctx, rays, n);
+  if (rc) return rc;
+  if (n > 0 && !occluded) return set_error(ctx, FLG_ERR_ARG, "occluded is NULL");
+  if (bvh->n_scenes != 1) return set_error(ctx, FLG_ERR_ARG, "batched handle: use flg_trace_closest_batched");
+  return trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, opts, nullptr, 1, nullptr, occluded);
+}
+
+FLG_API int flg_trace_closest_batched(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays,
+                                      const int64_t *ray_offsets_host, const flg_trace_opts *opts,
+                                      flg_hits *out) {
+  if (!ctx || !bvh || !out || !ray_offsets_host)
+    return ctx ? set_error(ctx, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
+  const int ns = bvh->n_scenes;
+  if (ray_offsets_host[0] != 0) return set_error(ctx, FLG_ERR_ARG, "ray_offsets[0] must be 0");
+  for (int s = 0; s < ns; ++s)
+    if (ray_offsets_host[s + 1] < ray_offsets_host[s])
+      return set_error(ctx, FLG_ERR_ARG, "ray_offsets must be non-decreasing");
+  const int64_t n = ray_offsets_host[ns];
+  int rc = check_rays(ctx, rays, n);
+  if (rc) return rc;
+  if (n > 0 && (!out->prim || !out->t || !out->u || !out->v))
+    return set_error(ctx, FLG_ERR_ARG, "hit output pointer is NULL");
+  // Device copy of the offsets, refreshed only when they change (so a
+  // captured graph replays without a host copy).
+  static thread_local std::vector<int64_t> cached;
+  bool same = ctx->d_ray_off && ctx->ray_off_cap >= ns + 1 && cached.size() == (size_t)(ns + 1) &&
+              std::equal(cached.begin(), cached.end(), ray_offsets_host);
+  if (!same) {
+    if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "new ray offsets inside a capture; call once before");
+    if (ctx->ray_off_cap < ns + 1) {
+      cudaFree(ctx->d_ray_off);
+      FLG_CUDA(ctx, cudaMalloc((void **)&ctx->d_ray_off, sizeof(int64_t) * (ns + 1)));
+      ctx->ray_off_cap = ns + 1;
+    }
+    FLG_CUDA(ctx, cudaMemcpy(ctx->d_ray_off, ray_offsets_host, sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice));
+    cached.assign(ray_offsets_host, ray_offsets_host + ns + 1);
+  }
+  return trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, opts, ctx->d_ray_off, ns, out, nullptr);
+}
+
+// Host-buffer entry point: chunks of rays are staged through device buffers
+// on two streams so that host->device copies, traversal and device->host
+// copies of neighbouring chunks overlap.
+FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *rh, int64_t n,
+                                   const flg_trace_opts *opts, flg_hits *oh) {
+  if (!ctx || !bvh || !oh) return ctx ? set_error(ctx, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
+  int rc = check_rays(ctx, rh, n);
+  if (rc) return rc;
+  if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "host staging cannot be captured");
+  if (bvh->n_scenes != 1) return set_error(ctx, FLG_ERR_ARG, "batched handle");
+  if (n > 0 && (!oh->prim || !oh->t || !oh->u || !oh->v))
+    return set_error(ctx, FLG_ERR_ARG, "hit output pointer is NULL");
+  if ((rc = ensure_trace_scratch(ctx))) return rc;
+  const int64_t chunk = std::min<int64_t>(n, (int64_t)1 << 22);
+  if (chunk == 0) return FLG_OK;
+  // Per buffer: 8 ray arrays + 4 hit arrays, 4 bytes each.
+  const size_t per_buf = (size_t)chunk * 12 * sizeof(float);
+  if (ctx->stage_bytes < 2 * per_buf) {
+    cudaFree(ctx->stage);
+    ctx->stage = nullptr;
+    ctx->stage_bytes = 0;
+    FLG_CUDA(ctx, cudaMalloc(&ctx->stage, 2 * per_buf));
+    ctx->stage_bytes = 2 * per_buf;
+  }
+  cudaStream_t ss[2] = {ctx->stream, ctx->copy_stream};
+  // The second stream must not start before earlier work on the main stream.
+  FLG_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+  FLG_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[0], 0));
+  for (int64_t c0 = 0, ci = 0; c0 < n; c0 += chunk, ++ci) {
+    const int k = (int)(ci & 1);
+    const int64_t m = std::min(chunk, n - c0);
+    cudaStream_t st = ss[k];
+    float *base = (float *)((char *)ctx->stage + k * per_buf);
+    float *arr[12];
+    for (int a = 0; a < 12; ++a) arr[a] = base + (size_t)a * chunk;
+    const float *src[8] = {rh->ox, rh->oy, rh->oz, rh->dx, rh->dy, rh->dz, rh->tmin, rh->tmax};
+    for (int a = 0; a < 8; ++a)
+      if (src[a]) FLG_CUDA(ctx, cudaMemcpyAsync(arr[a], src[a] + c0, sizeof(float) * m, cudaMemcpyHostToDevice, st));
+    flg_rays dr{arr[0], arr[1], arr[2], arr[3], arr[4], arr[5], rh->tmin ? arr[6] : nullptr,
+                rh->tmax ? arr[7] : nullptr, rh->tmin_const, rh->tmax_const};
+    flg_hits dh{(int32_t *)arr[8], arr[9], arr[10], arr[11]};
+    flg_trace_opts op{};
+    if (opts) op = *opts;
+    op.persistent = 0;
+    rc = trace_enqueue(ctx, st, k, bvh, &dr, m, &op, nullptr, 1, &dh, nullptr);
+    if (rc) return rc;
+    FLG_CUDA(ctx, cudaMemcpyAsync(oh->prim + c0, dh.prim, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st));
+    FLG_CUDA(ctx, cudaMemcpyAsync(oh->t + c0, dh.t, sizeof(float) * m, cudaMemcpyDeviceToHost, st));
+    FLG_CUDA(ctx, cudaMemcpyAsync(oh->u + c0, dh.u, sizeof(float) * m, cudaMemcpyDeviceToHost, st));
+    FLG_CUDA(ctx, cudaMemcpyAsync(oh->v + c0, dh.v, sizeof(float) * m, cudaMemcpyDeviceToHost, st));
+  }
+  FLG_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+  FLG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return flg_ctx_sync(ctx);
+}
+
+FLG_API int flg_autotune_trace(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n, flg_trace_opts *best,
+                               int32_t *best_width, char *json, size_t json_len) {
+  if (!ctx || !bvh || !best) return FLG_ERR_ARG;
+  int rc = check_rays(ctx, rays, n);
+  if (rc) return rc;
+  if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "autotuning cannot be captured");
+  if (bvh->n_scenes != 1) return set_error(ctx, FLG_ERR_ARG, "autotune a single-scene handle");
+  // Scratch outputs.
+  void *buf = nullptr;
+  FLG_CUDA(ctx, cudaMalloc(&buf, sizeof(float) * 4 * (size_t)std::max<int64_t>(n, 1)));
+  flg_hits h{(int32_t *)buf, (float *)buf + n, (float *)buf + 2 * n, (float *)buf + 3 * n};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  std::string rec = "{\"trials\": [";
+  float best_ms = 1e30f;
+  flg_trace_opts bo{};
+  int bw = bvh->width, bl = bvh->leaf_size;
+  const int orig_w = bvh->width, orig_leaf = bvh->leaf_size;
+  bool first = true;
+  for (int w : {2, 4, 8}) {
+    for (int leaf : (w == 2 ? std::initializer_list<int>{1} : std::initializer_list<int>{1, 2, 4})) {
+      rc = flg_bvh_set_width(ctx, bvh, w, leaf);
+      if (rc) goto done;
+      for (int stack : {32, 64}) {
+        if (w == 2 && stack == 32) continue;
+        for (int pers : {0, 1}) {
+          if (w == 2 && pers) continue;
+          for (int refill : (pers ? std::initializer_list<int>{8, 16, 24} : std::initializer_list<int>{0})) {
+            for (int threads : {128, 256}) {
+              flg_trace_opts op{};
+              op.stack_depth = stack;
+              op.persistent = pers;
+              op.refill_lanes = refill ? refill : 16;
+              op.block_threads = threads;
+              // warm-up + 3 timed runs, median-free mean
+              rc = trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, &op, nullptr, 1, &h, nullptr);
+              if (rc) goto done;
+              cudaEventRecord(e0, ctx->stream);
+              for (int r = 0; r < 3 && !rc; ++r)
+                rc = trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, &op, nullptr, 1, &h, nullptr);
+              if (rc) goto done;
+              cudaEventRecord(e1, ctx->stream);
+              cudaEventSynchronize(e1);
+              float ms = 0.0f;
+              cudaEventElapsedTime(&ms, e0, e1);
+              ms /= 3.0f;
+              char line[256];
+              snprintf(line, sizeof(line),
+                       "%s{\"node_width\": %d, \"leaf_size\": %d, \"stack_depth\": %d, \"persistent\": %d, "
+                       "\"refill_lanes\": %d, \"block_threads\": %d, \"ms\": %.5f, \"mrays_s\": %.2f}",
+                       first ? "" : ", ", w, leaf, stack, pers, op.refill_lanes, threads, ms,
+                       n / (ms * 1e3));
+              first = false;
+              rec += line;
+              if (ms < best_ms) {
+                best_ms = ms;
+                bo = op;
+                bw = w;
+                bl = leaf;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  {
+    int best_leaf = bl;
+    rc = flg_bvh_set_width(ctx, bvh, bw, best_leaf);
+    char tail[256];
+    snprintf(tail, sizeof(tail),
+             "], \"best\": {\"node_width\": %d, \"leaf_size\": %d, \"stack_depth\": %d, \"persistent\": %d, "
+             "\"refill_lanes\": %d, \"block_threads\": %d, \"ms\": %.5f}}",
+             bw, best_leaf, bo.stack_depth, bo.persistent, bo.refill_lanes, bo.block_threads, best_ms);
+    rec += tail;
+  }
+done:
+  (void)orig_w;
+  (void)orig_leaf;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (rc) return rc;
+  *best = bo;
+  if (best_width) *best_width = bw;
+  if (json && json_len) {
+    std::strncpy(json, rec.c_str(), json_len - 1);
+    json[json_len - 1] = '\0';
+  }
+  return flg_ctx_sync(ctx);
+}

@@ -1,0 +1,282 @@
+/*
+ * flg.h — C ABI of the GB300 acceleration-structure and participating-media
+ * library (libflg.so).
+ *
+ * The library replaces, for one GPU, these reference interfaces (paths are
+ * relative to the fledge project root):
+ *   - BVHBuilderBase::build / getBound / intersect(BVHRayHit&)
+ *       src/experimental/base_bvh.hpp:105-117, implemented by
+ *       RadixBVHBuilder (src/experimental/radix_bvh.hpp:32-84,
+ *       src/experimental/radix_bvh.cpp:18-245)
+ *   - Primitive::intersect / getBound and Accel (src/primitive.hpp:26-72,
+ *       src/accel.hpp:12-54) — closest hit that shortens ray.m_tMax
+ *   - Volume::tr / Volume::sample (src/volume.hpp:16-30), implemented by
+ *       OpenVDBVolume::tr / sample (src/volume.cpp:75-148)
+ *
+ * Conventions
+ *   - Every call returns an int status (flg_status).  No exception and no
+ *     abort crosses the ABI; the reference's SErr/assert aborts become codes.
+ *   - Device pointers unless a name ends in _host.  Buffers are owned by the
+ *     caller; handles own what they allocate.
+ *   - Calls are ordered on the context's stream and return without
+ *     synchronising unless documented otherwise.  flg_ctx_sync() waits and
+ *     reports device-side errors (bounded waits that timed out, traversal
+ *     stack overflow).
+ *   - One flg_ctx per host thread; handles may be shared read-only between
+ *     contexts on the same device once built.
+ */
+#ifndef FLG_H_
+#define FLG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define FLG_API extern "C" __attribute__((visibility("default")))
+#else
+#define FLG_API extern __attribute__((visibility("default")))
+#endif
+
+typedef enum flg_status {
+  FLG_OK = 0,
+  FLG_ERR_ARG = 1,         /* bad pointer, size or option; nothing launched */
+  FLG_ERR_OOM = 2,         /* a device or pinned-host allocation failed */
+  FLG_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  FLG_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  FLG_ERR_STACK = 5,       /* traversal stack overflow (all stack sizes tried) */
+  FLG_ERR_STATE = 6,       /* call not valid in the current state */
+  FLG_ERR_UNSUPPORTED = 7  /* option not implemented */
+} flg_status;
+
+typedef struct flg_ctx_t *flg_ctx;
+typedef struct flg_bvh_t *flg_bvh;
+typedef struct flg_grid_t *flg_grid;
+typedef struct flg_graph_t *flg_graph;
+
+/* Rays, structure of arrays, n entries each.  tmin / tmax may be NULL, in
+ * which case every ray uses tmin_const / tmax_const.  The reference's
+ * BVHRayHit (base_bvh.hpp:41-50) holds ray_o, ray_d, tnear, tfar. */
+typedef struct flg_rays {
+  const float *ox, *oy, *oz;
+  const float *dx, *dy, *dz;
+  const float *tmin, *tmax;
+  float tmin_const, tmax_const;
+} flg_rays;
+
+/* Closest-hit results, structure of arrays.  prim is the original index of
+ * the triangle within its scene (-1 = miss); t is the hit distance (tmax on a
+ * miss); u, v are barycentrics with P = (1-u-v) p0 + u p1 + v p2. */
+typedef struct flg_hits {
+  int32_t *prim;
+  float *t, *u, *v;
+} flg_hits;
+
+typedef struct flg_build_opts {
+  int32_t node_width;     /* traversal layout: 2, 4 or 8 (0 = 4) */
+  int32_t leaf_size;      /* wide layouts: max triangles per leaf range (0 = 1) */
+  int32_t keep_topology;  /* keep the Karras arrays for flg_bvh_download */
+} flg_build_opts;
+
+typedef struct flg_trace_opts {
+  int32_t stack_depth;    /* 32 or 64 (0 = 64); overflowing rays are retried deeper */
+  int32_t block_threads;  /* threads per block (0 = 256) */
+  int32_t persistent;     /* 1: persistent work-stealing kernel, 0: one ray per thread */
+  int32_t refill_lanes;   /* persistent: refill a warp once this many lanes idle (0 = 16) */
+  int32_t ray_sort;       /* 0: none; 1: sort rays by direction octant and origin cell */
+} flg_trace_opts;
+
+/* ------------------------------- context -------------------------------- */
+
+/* Creates a context on `device` that issues work on `stream` (a cudaStream_t;
+ * NULL creates a private non-blocking stream). */
+FLG_API int flg_ctx_create(int32_t device, void *stream, flg_ctx *out);
+FLG_API int flg_ctx_destroy(flg_ctx ctx);
+/* Waits for the context's stream and returns the first device-side error
+ * recorded since the previous sync (FLG_ERR_TIMEOUT, FLG_ERR_STACK). */
+FLG_API int flg_ctx_sync(flg_ctx ctx);
+FLG_API void *flg_ctx_stream(flg_ctx ctx);
+/* Number of kernels the library has launched through this context (each
+ * launch of a captured graph counts the kernels once, at capture). */
+FLG_API int64_t flg_ctx_launch_count(flg_ctx ctx);
+/* Test hook: caps every bounded device-side spin-wait at `spins` iterations
+ * (0 restores the default).  Used to inject FLG_ERR_TIMEOUT from the host. */
+FLG_API int flg_ctx_set_spin_limit(flg_ctx ctx, uint32_t spins);
+FLG_API const char *flg_status_string(int status);
+/* Test hook: launches one thread that waits, with the library's bounded
+ * spin-wait, on a device word that nothing ever sets, then synchronises.
+ * Returns FLG_ERR_TIMEOUT after `spins` polls and leaves the context usable. */
+FLG_API int flg_debug_wait_unset_flag(flg_ctx ctx, uint32_t spins);
+/* Copies the last error message of the context into buf (NUL-terminated). */
+FLG_API int flg_ctx_last_error(flg_ctx ctx, char *buf, size_t len);
+
+/* --------------------------------- build -------------------------------- */
+
+/* Karras LBVH of one triangle mesh (RadixBVHBuilder::build,
+ * radix_bvh.cpp:18-24,32-200).  pos: 3*n_vert floats (xyz interleaved).  idx:
+ * 3*n_tri vertex indices, or NULL for a triangle soup (vertex k of triangle i
+ * is 3i+k, n_vert = 3 n_tri).  The mesh arrays are borrowed, not copied, as
+ * in the reference (radix_bvh.cpp:42-45): they must outlive the handle. */
+FLG_API int flg_bvh_build(flg_ctx ctx, const float *pos, const int32_t *idx, int64_t n_tri,
+                          int64_t n_vert, const flg_build_opts *opts, flg_bvh *out);
+
+/* Many independent scenes built in one segmented pass.  Scene s owns
+ * triangles [tri_offsets_host[s], tri_offsets_host[s+1]) of the shared
+ * arrays; with idx != NULL indices are global vertex indices. */
+FLG_API int flg_bvh_build_batched(flg_ctx ctx, const float *pos, const int32_t *idx,
+                                  const int64_t *tri_offsets_host, int32_t n_scenes,
+                                  int64_t n_vert, const flg_build_opts *opts, flg_bvh *out);
+
+/* Rebuilds an existing handle over new vertex positions of the same size
+ * without allocating (usable inside a CUDA graph capture). */
+FLG_API int flg_bvh_rebuild(flg_ctx ctx, flg_bvh bvh, const float *pos);
+
+FLG_API int flg_bvh_destroy(flg_bvh bvh);
+
+typedef struct flg_bvh_info {
+  int64_t n_tri;          /* all scenes */
+  int32_t n_scenes;
+  int32_t node_width;
+  int64_t n_wide_nodes;
+  int64_t device_bytes;   /* memory held by the handle */
+  float bound[6];         /* scene 0: lower xyz, upper xyz (getBound()) */
+} flg_bvh_info;
+FLG_API int flg_bvh_info_get(flg_bvh bvh, flg_bvh_info *out);
+
+/* Karras arrays of one scene, for parity checks (synchronous).  Host
+ * pointers; NULL members are skipped.  Internal nodes are numbered as in the
+ * reference (root = 0, children split and split+1). */
+typedef struct flg_bvh_topology {
+  uint32_t *morton;       /* n: sorted Morton codes */
+  int32_t *perm;          /* n: sorted position -> original triangle */
+  int32_t *split;         /* n-1 */
+  uint8_t *leaf_flags;    /* n-1: bit0 left child is a leaf, bit1 right */
+  int32_t *range_j;       /* n-1: other end j of the node's range */
+  int32_t *parent;        /* n-1: internal-node parents (root: 0) */
+  int32_t *leaf_parent;   /* n */
+  float *bounds;          /* 6(n-1): node bound lower xyz, upper xyz */
+  float *scene_bound;     /* 6: union of triangle bounds (Morton frame) */
+} flg_bvh_topology;
+FLG_API int flg_bvh_download(flg_bvh bvh, int32_t scene, flg_bvh_topology *out);
+
+/* ------------------------------- traversal ------------------------------ */
+
+/* Closest hit (RadixBVHBuilder::intersect, radix_bvh.cpp:26-30,202-245, with
+ * the watertight Pluecker test of intersector.hpp:63-101).  A hit counts if
+ * tmin <= t <= tmax; among equal t the first found is kept. */
+FLG_API int flg_trace_closest(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n,
+                              const flg_trace_opts *opts, flg_hits *out);
+
+/* Any hit (IntersectP; no counterpart in the reference, whose shadow rays use
+ * closest hit, integrator.cpp:29-37): occluded[i] = 1 if any triangle is hit
+ * with tmin <= t <= tmax. */
+FLG_API int flg_trace_any(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n,
+                          const flg_trace_opts *opts, uint8_t *occluded);
+
+/* Batched: rays [ray_offsets_host[s], ray_offsets_host[s+1]) go to scene s of
+ * a batched handle; one persistent launch traces all scenes. */
+FLG_API int flg_trace_closest_batched(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays,
+                                      const int64_t *ray_offsets_host,
+                                      const flg_trace_opts *opts, flg_hits *out);
+
+/* Same as flg_trace_closest with host (preferably pinned) buffers: the call
+ * stages rays to the device in chunks, traces and copies hits back, with
+ * copies and kernels overlapped on two streams.  Synchronous. */
+FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays_host,
+                                   int64_t n, const flg_trace_opts *opts, flg_hits *out_host);
+
+/* Sweeps node width (2/4/8), stack depth (32/64), persistent kernel on/off
+ * with refill thresholds and ray sorting on the given workload, keeps the
+ * fastest in *best and writes a JSON record (NUL-terminated) to json_out. */
+FLG_API int flg_autotune_trace(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n,
+                               flg_trace_opts *best, int32_t *best_node_width, char *json_out,
+                               size_t json_len);
+
+/* Re-lays out the traversal nodes of a built handle at another width. */
+FLG_API int flg_bvh_set_width(flg_ctx ctx, flg_bvh bvh, int32_t node_width, int32_t leaf_size);
+
+/* -------------------------------- adjoint ------------------------------- */
+
+/* Gradient of (t, u, v) of fixed hits with respect to the vertex positions
+ * (no counterpart in the reference).  dL_dt/du/dv: n floats (NULL = 0).
+ * dL_dpos: 3*n_vert floats, accumulated with fp32 atomics. */
+FLG_API int flg_hit_adjoint(flg_ctx ctx, const float *pos, const int32_t *idx, int64_t n_tri,
+                            int64_t n_vert, const flg_rays *rays, int64_t n,
+                            const flg_hits *hits, const float *dL_dt, const float *dL_du,
+                            const float *dL_dv, float *dL_dpos);
+
+/* ------------------------------- volumes -------------------------------- */
+
+typedef struct flg_medium {
+  float sigma_s;       /* scattering per unit density */
+  float sigma_a;       /* absorption per unit density */
+  float g;             /* Henyey-Greenstein asymmetry */
+  float rr_threshold;  /* ratio-tracking roulette threshold (0.1 in volume.cpp:98); 0 disables */
+  float majorant;      /* <= 0: maximum grid value (volume.cpp:52-59) */
+} flg_medium;
+
+/* Dense density grid: nx*ny*nz fp32 samples (x fastest) at the vertices of a
+ * regular lattice spanning [box_lo, box_hi]; trilinear interpolation,
+ * background 0 outside.  density is borrowed. */
+FLG_API int flg_grid_create(flg_ctx ctx, const float *density, int32_t nx, int32_t ny, int32_t nz,
+                            const float *box_lo_host, const float *box_hi_host,
+                            const flg_medium *medium, flg_grid *out);
+FLG_API int flg_grid_destroy(flg_grid grid);
+FLG_API int flg_grid_majorant(flg_grid grid, float *majorant_host);
+
+/* Per-ray state after the last Russian-roulette survival (t, draw counter,
+ * transmittance): the adjoint's checkpoint, 12 bytes per ray. */
+typedef struct flg_tr_ckpt {
+  float *t;
+  uint32_t *k;
+  float *c;
+} flg_tr_ckpt;
+
+/* Ratio-tracking transmittance (OpenVDBVolume::tr, volume.cpp:75-107).  Ray i
+ * draws from Philox-4x32-10 stream (seed, i).  ckpt may be NULL. */
+FLG_API int flg_volume_tr(flg_ctx ctx, flg_grid grid, const flg_rays *rays, int64_t n,
+                          uint64_t seed, float *T, const flg_tr_ckpt *ckpt);
+
+/* Adjoint of flg_volume_tr: dL_dgrid += sum_i dL_dT[i] dT_i/dgrid, majorant
+ * held constant.  T is the forward output.  With ckpt == NULL each ray's
+ * forward is replayed to find its last roulette segment. */
+FLG_API int flg_volume_tr_adjoint(flg_ctx ctx, flg_grid grid, const flg_rays *rays, int64_t n,
+                                  uint64_t seed, const float *dL_dT, const float *T,
+                                  const flg_tr_ckpt *ckpt, float *dL_dgrid);
+
+/* Delta tracking (OpenVDBVolume::sample, volume.cpp:109-148): success[i],
+ * collision point p (3n floats, xyz interleaved), weight sigma_s/sigma_t on a
+ * collision, 1 otherwise. */
+FLG_API int flg_volume_sample(flg_ctx ctx, flg_grid grid, const flg_rays *rays, int64_t n,
+                              uint64_t seed, uint8_t *success, float *p, float *weight);
+
+/* ----------------------------- CUDA graphs ------------------------------ */
+
+/* Captures every library call issued on ctx between begin and end into a
+ * graph; calls that allocate are refused with FLG_ERR_STATE while capturing. */
+FLG_API int flg_graph_begin(flg_ctx ctx);
+FLG_API int flg_graph_end(flg_ctx ctx, flg_graph *out);
+FLG_API int flg_graph_launch(flg_ctx ctx, flg_graph graph);
+FLG_API int flg_graph_destroy(flg_graph graph);
+
+/* --------------------------- synthetic inputs ---------------------------- */
+/* Seeded generators of the benchmark workloads, on the device.  Philox
+ * streams keyed by seed; identical across runs. */
+
+/* Random triangle soup: centroid U[0,1]^3, vertices centroid + U[-r,r]^3.
+ * pos: 9 n_tri floats.  first_tri offsets the stream (batched scenes). */
+FLG_API int flg_gen_triangles(flg_ctx ctx, uint64_t seed, int64_t first_tri, int64_t n_tri,
+                              float half_extent, float *pos);
+/* Rays from a sphere of radius `radius` around `center` toward uniform points
+ * of [0,1]^3 (SoA device arrays ox..dz, each n). */
+FLG_API int flg_gen_rays(flg_ctx ctx, uint64_t seed, int64_t first_ray, int64_t n,
+                         const float *center_host, float radius, float *ox, float *oy, float *oz,
+                         float *dx, float *dy, float *dz);
+/* 4-octave value noise on an nx*ny*nz lattice over [0,1]^3, remapped to
+ * [0, scale]. */
+FLG_API int flg_gen_noise_grid(flg_ctx ctx, uint64_t seed, int32_t nx, int32_t ny, int32_t nz,
+                               float scale, float *density);
+
+/* Version string of the library. */
+FLG_API const char *flg_version(void);
+
+#endif /* FLG_H_ */

@@ -1,0 +1,1052 @@
+// oracle.cpp — CPU restatement of fledge's acceleration-structure and
+// participating-media hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU library in
+// fledge_gb300/: only tests/, __graft_entry__.smoke() and bench.py's CPU
+// baseline legs load it.  The product path never calls into it.
+//
+// Every function cites the reference source it restates (paths are relative
+// to the fledge project root).  The reference itself cannot be compiled here:
+// radix_bvh.cpp / base_bvh.hpp need TBB and Embree headers, volume.cpp needs
+// OpenVDB and debug.hpp needs fmt, none of which exist on this machine.
+// Parity status:
+//   * Morton codes, sorted order, Karras topology, refit bounds, Pluecker
+//     hit/miss and closest-hit selection: restated line by line; pinned only
+//     by the reference's own property tests (watertight mesh, two accelerators
+//     agree exactly) because the reference ships no golden vectors.
+//   * OpenVDB trilinear sampling and world transform: PARITY UNPINNED (the
+//     dense vertex-centred lattice below is this project's definition).
+//   * Embree / TBB: PARITY UNPINNED (absent); the TBB sort is unstable, the
+//     defined tie order is (code, original index).
+//
+// Arithmetic modes.  Compiled with -ffp-contract=off so that no multiply-add
+// is fused; every fp32 expression is evaluated exactly in the order written,
+// which is the order of the reference expressions (Dot = (x0*y0 + x1*y1) +
+// x2*y2, Cross as in common/vector.h:399-404).
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include <parallel/algorithm>
+
+#define ORC_API extern "C" __attribute__((visibility("default")))
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11).  The reference draws with std::mt19937
+// (rng.hpp:21-34); the hot path fixes per-ray counter-based streams instead so
+// that the adjoint can replay them.
+// ---------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+
+inline U4 philox(U4 c, uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)0xD2511F53u * c.x;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c.z;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+inline float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+// Free-flight loops stop after this many steps (same cap as the GPU kernels).
+constexpr int kMaxTrackSteps = 1 << 20;
+
+// Per-ray stream: draw k of ray r under seed s is word (k & 3) of
+// philox({k >> 2, r_lo, r_hi, 0x7e5}, {s_lo, s_hi}).
+struct RayStream {
+  uint32_t k0, k1, rlo, rhi;
+  uint32_t k = 0;
+  U4 block{};
+  uint32_t cached = 0xFFFFFFFFu;
+  float next() {
+    uint32_t b = k >> 2;
+    if (b != cached) {
+      block = philox(U4{b, rlo, rhi, 0x7e5u}, k0, k1);
+      cached = b;
+    }
+    uint32_t w = k & 3;
+    ++k;
+    uint32_t x = w == 0 ? block.x : w == 1 ? block.y : w == 2 ? block.z : block.w;
+    return u01(x);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Natural logarithm used by the free-path sampler.  The reference calls
+// std::log (volume.cpp:187,226); libm and the GPU's logf do not round alike,
+// so both sides use this restatement of the textbook reduction
+//   x = m * 2^e,  m in [sqrt(1/2), sqrt(2)),
+//   ln m = 2 atanh(s) = 2 (s + s^3/3 + s^5/5 + s^7/7 + s^9/9),  s=(m-1)/(m+1)
+// evaluated with plain IEEE fp32 operations, giving bit-identical step
+// lengths on host and device.
+// ---------------------------------------------------------------------------
+inline float flg_logf(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  int e = (int)(b >> 23) - 127;
+  uint32_t mb = (b & 0x007FFFFFu) | 0x3F800000u;
+  if (mb > 0x3FB504F3u) {  // m > sqrt(2)
+    mb -= 0x00800000u;
+    e += 1;
+  }
+  float m;
+  std::memcpy(&m, &mb, 4);
+  float s = (m - 1.0f) / (m + 1.0f);
+  float z = s * s;
+  float p = 0.11111111f;
+  p = p * z;
+  p = p + 0.14285715f;
+  p = p * z;
+  p = p + 0.2f;
+  p = p * z;
+  p = p + 0.33333334f;
+  p = p * z;
+  float sp = s * p;
+  float lnm = s + sp;
+  lnm = lnm + lnm;
+  float fe = (float)e;
+  float hi = fe * 0.693145752f;
+  float lo = fe * 1.42860677e-06f;
+  return hi + (lnm + lo);
+}
+
+// ---------------------------------------------------------------------------
+// Bounds (experimental/base_bvh.hpp:53-60, 90-102).
+// ---------------------------------------------------------------------------
+struct Bound {
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+  float hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  void merge(const Bound &o) {
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = std::min(lo[k], o.lo[k]);
+      hi[k] = std::max(hi[k], o.hi[k]);
+    }
+  }
+};
+
+struct Mesh {
+  const float *pos;
+  const int32_t *idx;  // nullptr: triangle soup, vertex k of tri i = 3i+k
+  int64_t n_tri;
+  const float *v(int64_t tri, int k) const {
+    int64_t vi = idx ? (int64_t)idx[3 * tri + k] : 3 * tri + k;
+    return pos + 3 * vi;
+  }
+  Bound bound(int64_t tri) const {
+    // BVHBuilderBase::Triangle::getBound (base_bvh.hpp:90-102)
+    const float *p0 = v(tri, 0), *p1 = v(tri, 1), *p2 = v(tri, 2);
+    Bound b;
+    for (int k = 0; k < 3; ++k) {
+      b.lo[k] = std::min(std::min(p0[k], p1[k]), p2[k]);
+      b.hi[k] = std::max(std::max(p0[k], p1[k]), p2[k]);
+    }
+    return b;
+  }
+};
+
+// experimental_utils.hpp:33-40 (LeftShift3) and :42-45 (EncodeMorton3)
+inline uint32_t left_shift3(uint32_t x) {
+  if (x == (1u << 10)) --x;
+  x = (x | (x << 16)) & 0x030000FFu;
+  x = (x | (x << 8)) & 0x0300F00Fu;
+  x = (x | (x << 4)) & 0x030C30C3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+
+// float -> uint32 conversion of the normalised coordinate (the implicit
+// conversion at experimental_utils.hpp:43-44).  A zero-extent axis divides 0
+// by 0 in the reference (undefined conversion); here it is defined as 0.
+inline uint32_t to_u32(float v) {
+  if (!(v > 0.0f)) return 0u;
+  return (uint32_t)v;
+}
+
+// radix_bvh.cpp:63-73 (prestage Morton loop)
+inline uint32_t morton_of(const Bound &tb, const Bound &scene) {
+  float e[3], n[3];
+  for (int k = 0; k < 3; ++k) {
+    e[k] = scene.hi[k] - scene.lo[k];
+    float c = (tb.lo[k] + tb.hi[k]) / 2.0f;
+    n[k] = e[k] == 0.0f ? 0.0f : (c - scene.lo[k]) / e[k];
+    n[k] = n[k] * 1024.0f;
+  }
+  return (left_shift3(to_u32(n[2])) << 2) | (left_shift3(to_u32(n[1])) << 1) |
+         left_shift3(to_u32(n[0]));
+}
+
+// experimental_utils.hpp:27-31: pow(2, ceil(log2(n))) for n >= 1
+inline int next2pow(int n) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+struct Karras {
+  const uint32_t *code;
+  int n;
+  // radix_bvh.hpp:68-74
+  inline int delta(int i, int j) const {
+    if (j < 0 || j >= n) return -1;
+    if (code[i] == code[j]) return __builtin_clz((uint32_t)(i ^ j)) + 32;
+    return __builtin_clz(code[i] ^ code[j]);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Pluecker ray/triangle test (experimental/intersector.hpp:45-101).
+// Mode REF: the reference formula; the normal is normalised in double with
+//   the Euclidean norm.  The reference's StableNormalize (common/vector.h:
+//   495-503) adds z instead of z*z; mode DEFECT restates that literally, which
+//   yields a NaN normal (and a miss) whenever x*x + y*y + 2z < 0.
+// Mode DEV: the same test with the normal left unnormalised; this is the
+//   arithmetic the GPU kernels use (the factor 2 of Twice() cancels exactly).
+// u = U/(U+V+W), v = V/(U+V+W) (Embree's barycentric convention; the reference
+// computes U, V, W but returns no barycentrics).
+// ---------------------------------------------------------------------------
+enum { MODE_REF = 0, MODE_DEFECT = 1, MODE_DEV = 2 };
+
+struct V3 { float x, y, z; };
+inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline V3 ld3(const float *p) { return {p[0], p[1], p[2]}; }
+
+// intersector.hpp:45-60
+inline V3 stable_triangle_normal(V3 a, V3 b, V3 c) {
+  float ab_x = a.z * b.y, ab_y = a.x * b.z, ab_z = a.y * b.x;
+  float bc_x = b.z * c.y, bc_y = b.x * c.z, bc_z = b.y * c.x;
+  V3 cab = {a.y * b.z - ab_x, a.z * b.x - ab_y, a.x * b.y - ab_z};
+  V3 cbc = {b.y * c.z - bc_x, b.z * c.x - bc_y, b.x * c.y - bc_z};
+  return {std::fabs(ab_x) < std::fabs(bc_x) ? cab.x : cbc.x,
+          std::fabs(ab_y) < std::fabs(bc_y) ? cab.y : cbc.y,
+          std::fabs(ab_z) < std::fabs(bc_z) ? cab.z : cbc.z};
+}
+
+struct Hit { float t, u, v; };
+
+inline bool pluecker(V3 a, V3 b, V3 c, V3 O, V3 D, int mode, Hit *h) {
+  V3 v0 = sub(a, O), v1 = sub(b, O), v2 = sub(c, O);
+  V3 e0 = sub(v2, v0), e1 = sub(v0, v1), e2 = sub(v1, v2);
+  float U = dot(cross(e0, add(v2, v0)), D);
+  float V = dot(cross(e1, add(v0, v1)), D);
+  float W = dot(cross(e2, add(v1, v2)), D);
+  float UVW = U + V + W;
+  float eps = FLT_EPSILON * std::fabs(UVW);
+  bool valid = std::min(U, std::min(V, W)) >= -eps || std::max(U, std::max(V, W)) <= eps;
+  if (!valid) return false;
+  V3 Ng = stable_triangle_normal(e0, e1, e2);
+  if (mode != MODE_DEV) {
+    double x = Ng.x, y = Ng.y, z = Ng.z;
+    double sq = mode == MODE_DEFECT ? x * x + y * y + z + z : x * x + y * y + z * z;
+    double r = std::sqrt(sq);
+    Ng = {(float)(x / r), (float)(y / r), (float)(z / r)};
+  }
+  float den = dot(Ng, D);
+  den = den + den;
+  float T = dot(v0, Ng);
+  T = T + T;
+  float t = T / den;
+  if (!(0.0f <= t)) return false;
+  if (!(den != 0.0f)) return false;
+  h->t = t;
+  h->u = UVW != 0.0f ? U / UVW : 0.0f;
+  h->v = UVW != 0.0f ? V / UVW : 0.0f;
+  return true;
+}
+
+// Same test in double precision end to end (the FP64 oracle for t, u, v).
+inline bool pluecker64(const float *fa, const float *fb, const float *fc, const double *O,
+                       const double *D, double *t, double *u, double *v) {
+  double a[3], b[3], c[3], v0[3], v1[3], v2[3], e0[3], e1[3], e2[3];
+  for (int k = 0; k < 3; ++k) {
+    a[k] = fa[k]; b[k] = fb[k]; c[k] = fc[k];
+    v0[k] = a[k] - O[k]; v1[k] = b[k] - O[k]; v2[k] = c[k] - O[k];
+  }
+  for (int k = 0; k < 3; ++k) {
+    e0[k] = v2[k] - v0[k]; e1[k] = v0[k] - v1[k]; e2[k] = v1[k] - v2[k];
+  }
+  auto crs = [](const double *p, const double *q, double *r) {
+    r[0] = p[1] * q[2] - p[2] * q[1];
+    r[1] = p[2] * q[0] - p[0] * q[2];
+    r[2] = p[0] * q[1] - p[1] * q[0];
+  };
+  auto dt = [](const double *p, const double *q) { return p[0] * q[0] + p[1] * q[1] + p[2] * q[2]; };
+  double s0[3], s1[3], s2[3], cr[3];
+  for (int k = 0; k < 3; ++k) { s0[k] = v2[k] + v0[k]; s1[k] = v0[k] + v1[k]; s2[k] = v1[k] + v2[k]; }
+  crs(e0, s0, cr); double U = dt(cr, D);
+  crs(e1, s1, cr); double V = dt(cr, D);
+  crs(e2, s2, cr); double W = dt(cr, D);
+  double S = U + V + W;
+  double N[3];
+  crs(e0, e1, N);
+  double den = dt(N, D);
+  if (den == 0.0 || S == 0.0) return false;
+  *t = dt(v0, N) / den;
+  *u = U / S;
+  *v = V / S;
+  return true;
+}
+
+// BoundIntersect (intersector.hpp:103-120): t0 starts at 0, t1 at FLT_MAX.
+inline bool bound_intersect(const float *lo, const float *hi, const float *o, const float *inv,
+                            float *tnear) {
+  float t0 = 0.0f, t1 = FLT_MAX;
+  for (int i = 0; i < 3; ++i) {
+    float tn = (lo[i] - o[i]) * inv[i];
+    float tf = (hi[i] - o[i]) * inv[i];
+    if (tn > tf) std::swap(tn, tf);
+    t0 = tn > t0 ? tn : t0;
+    t1 = tf < t1 ? tf : t1;
+    if (t0 > t1) return false;
+  }
+  *tnear = t0;
+  return true;
+}
+
+struct Tree {
+  int64_t n;
+  const int32_t *perm;      // sorted position -> original triangle
+  const int32_t *split;     // n-1
+  const uint8_t *leaf;      // n-1: bit0 left child is a leaf, bit1 right child
+  const float *nb;          // 6*(n-1): node bound lo xyz hi xyz
+};
+
+struct RayIn {
+  float o[3], d[3], inv[3], tmin, tmax;
+};
+
+struct Best {
+  float tfar;
+  int32_t prim;
+  float u, v;
+};
+
+// radix_bvh.cpp:202-245 (recursiveIntersect), extended with tmin, prim id and
+// barycentrics.  Leaves are tested left then right; a hit is kept unless
+// thit > tfar, so an equal-t hit found later replaces the earlier one.
+void recursive_intersect(const Tree &T, const Mesh &M, int node, const RayIn &r, int mode, Best &b) {
+  float tnear;
+  const float *nb = T.nb + 6 * (int64_t)node;
+  if (!bound_intersect(nb, nb + 3, r.o, r.inv, &tnear)) return;
+  if (b.tfar < tnear) return;
+  int s = T.split[node];
+  uint8_t lf = T.leaf[node];
+  V3 O = ld3(r.o), D = ld3(r.d);
+  for (int side = 0; side < 2; ++side) {
+    if (!(lf & (1 << side))) continue;
+    int tri = T.perm[s + side];
+    Hit h;
+    if (!pluecker(ld3(M.v(tri, 0)), ld3(M.v(tri, 1)), ld3(M.v(tri, 2)), O, D, mode, &h)) continue;
+    if (h.t > b.tfar) continue;
+    if (h.t < r.tmin) continue;
+    b.tfar = h.t;
+    b.prim = tri;
+    b.u = h.u;
+    b.v = h.v;
+  }
+  if (!(lf & 1)) recursive_intersect(T, M, s, r, mode, b);
+  if (!(lf & 2)) recursive_intersect(T, M, s + 1, r, mode, b);
+}
+
+// Any-hit: the reference has no IntersectP (shadow rays use closest-hit,
+// integrator.cpp:29-37); this terminates at the first accepted hit in
+// [tmin, tmax] using the same node and triangle tests.
+bool recursive_occluded(const Tree &T, const Mesh &M, int node, const RayIn &r, int mode) {
+  float tnear;
+  const float *nb = T.nb + 6 * (int64_t)node;
+  if (!bound_intersect(nb, nb + 3, r.o, r.inv, &tnear)) return false;
+  if (r.tmax < tnear) return false;
+  int s = T.split[node];
+  uint8_t lf = T.leaf[node];
+  V3 O = ld3(r.o), D = ld3(r.d);
+  for (int side = 0; side < 2; ++side) {
+    if (!(lf & (1 << side))) continue;
+    int tri = T.perm[s + side];
+    Hit h;
+    if (!pluecker(ld3(M.v(tri, 0)), ld3(M.v(tri, 1)), ld3(M.v(tri, 2)), O, D, mode, &h)) continue;
+    if (h.t > r.tmax || h.t < r.tmin) continue;
+    return true;
+  }
+  if (!(lf & 1) && recursive_occluded(T, M, s, r, mode)) return true;
+  if (!(lf & 2) && recursive_occluded(T, M, s + 1, r, mode)) return true;
+  return false;
+}
+
+inline RayIn make_ray(const float *rays, int64_t i, int64_t n) {
+  // rays: SoA of 8 arrays of n floats: ox oy oz dx dy dz tmin tmax
+  RayIn r;
+  for (int k = 0; k < 3; ++k) {
+    r.o[k] = rays[k * n + i];
+    r.d[k] = rays[(3 + k) * n + i];
+    r.inv[k] = 1.0f / r.d[k];
+  }
+  r.tmin = rays[6 * n + i];
+  r.tmax = rays[7 * n + i];
+  return r;
+}
+
+// ---------------------------------------------------------------------------
+// Dense density grid (restatement of OpenVDBVolume's sampling, volume.cpp:
+// 33-70, 94): a vertex-centred lattice of nx*ny*nz samples spanning the box,
+// x fastest; trilinear interpolation; lattice points outside the grid read
+// the background value 0.
+// ---------------------------------------------------------------------------
+struct Grid {
+  const float *rho;
+  int nx, ny, nz;
+  float lo[3], hi[3], scale[3];
+  float sigma_s, sigma_a, sigma_t, g;
+  float maxd, inv_maxd, rr;
+
+  inline float at(int x, int y, int z) const {
+    if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) return 0.0f;
+    return rho[((int64_t)z * ny + y) * nx + x];
+  }
+  // Returns the density; fills the corner base and fractions for the adjoint.
+  inline float sample(const float *p, int *base, float *f) const {
+    float gx = (p[0] - lo[0]) * scale[0];
+    float gy = (p[1] - lo[1]) * scale[1];
+    float gz = (p[2] - lo[2]) * scale[2];
+    float fx0 = std::floor(gx), fy0 = std::floor(gy), fz0 = std::floor(gz);
+    int x = (int)fx0, y = (int)fy0, z = (int)fz0;
+    float fx = gx - fx0, fy = gy - fy0, fz = gz - fz0;
+    base[0] = x; base[1] = y; base[2] = z;
+    f[0] = fx; f[1] = fy; f[2] = fz;
+    auto lerp = [](float a, float b, float w) { return a + (b - a) * w; };
+    float c00 = lerp(at(x, y, z), at(x + 1, y, z), fx);
+    float c10 = lerp(at(x, y + 1, z), at(x + 1, y + 1, z), fx);
+    float c01 = lerp(at(x, y, z + 1), at(x + 1, y, z + 1), fx);
+    float c11 = lerp(at(x, y + 1, z + 1), at(x + 1, y + 1, z + 1), fx);
+    float c0 = lerp(c00, c10, fy);
+    float c1 = lerp(c01, c11, fy);
+    return lerp(c0, c1, fz);
+  }
+  inline double at64(int x, int y, int z, const double *r64) const {
+    if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) return 0.0;
+    return r64 ? r64[((int64_t)z * ny + y) * nx + x] : (double)rho[((int64_t)z * ny + y) * nx + x];
+  }
+};
+
+// AABB::intersect_pbrt (common/aabb.h:38-59), t1 starting at the ray's tMax.
+inline bool box_intersect_pbrt(const Grid &G, const float *o, const float *d, float tmax,
+                               float *t0o, float *t1o) {
+  float t0 = 0.0f, t1 = tmax;
+  for (int i = 0; i < 3; ++i) {
+    float inv = 1.0f / d[i];
+    float tn = (G.lo[i] - o[i]) * inv;
+    float tf = (G.hi[i] - o[i]) * inv;
+    if (tn > tf) std::swap(tn, tf);
+    t0 = tn > t0 ? tn : t0;
+    t1 = tf < t1 ? tf : t1;
+    if (t0 > t1) return false;
+  }
+  *t0o = t0;
+  *t1o = t1;
+  return true;
+}
+
+struct TrState {  // state after the last Russian-roulette survival
+  float t;
+  uint32_t k;
+  float c;
+};
+
+// OpenVDBVolume::tr (volume.cpp:75-107): ratio tracking with Russian roulette.
+float ratio_track(const Grid &G, const float *o, const float *d, float tmax, RayStream &rs,
+                  TrState *ck) {
+  float t_min, t_max;
+  if (ck) *ck = TrState{0.0f, 0u, 1.0f};
+  if (!box_intersect_pbrt(G, o, d, tmax, &t_min, &t_max)) return 1.0f;
+  float tr = 1.0f, t = std::max(t_min, 0.0f);
+  t_max = std::min(t_max, tmax);
+  float max_mu = G.sigma_t * G.maxd;
+  if (ck) *ck = TrState{t, rs.k, tr};
+  for (int step_ = 0; step_ < kMaxTrackSteps; ++step_) {
+    float u = rs.next();
+    t += -flg_logf(1.0f - u) / max_mu;
+    if (t >= t_max) break;
+    float pos[3] = {o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t};
+    int base[3];
+    float f[3];
+    float density = G.sample(pos, base, f);
+    tr *= 1.0f - std::max(0.0f, density * G.inv_maxd);
+    if (tr < G.rr) {
+      float q = std::max(0.05f, 1.0f - tr);
+      if (rs.next() < q) return 0.0f;
+      tr /= 1.0f - q;
+      if (ck) *ck = TrState{t, rs.k, tr};
+    }
+  }
+  return tr;
+}
+
+// Same estimator in double precision (the FP64 oracle); the random draws are
+// the same uniforms.  rho64 (optional) overrides the grid values.
+double ratio_track64(const Grid &G, const double *rho64, const float *o, const float *d, float tmax,
+                     RayStream &rs, int *n_rr) {
+  double t0 = 0.0, t1 = tmax;
+  for (int i = 0; i < 3; ++i) {
+    double inv = 1.0 / (double)d[i];
+    double tn = ((double)G.lo[i] - o[i]) * inv;
+    double tf = ((double)G.hi[i] - o[i]) * inv;
+    if (tn > tf) std::swap(tn, tf);
+    t0 = std::max(tn, t0);
+    t1 = std::min(tf, t1);
+    if (t0 > t1) return 1.0;
+  }
+  double tr = 1.0, t = std::max(t0, 0.0), t_max = std::min(t1, (double)tmax);
+  double max_mu = (double)G.sigma_t * (double)G.maxd;
+  double inv_maxd = 1.0 / (double)G.maxd;
+  double sc[3];
+  for (int k = 0; k < 3; ++k) sc[k] = (double)(G.nx * (k == 0) + G.ny * (k == 1) + G.nz * (k == 2) - 1) / ((double)G.hi[k] - G.lo[k]);
+  for (int step_ = 0; step_ < kMaxTrackSteps; ++step_) {
+    double u = rs.next();
+    t += -std::log(1.0 - u) / max_mu;
+    if (t >= t_max) break;
+    double g[3];
+    for (int k = 0; k < 3; ++k) g[k] = ((double)o[k] + (double)d[k] * t - G.lo[k]) * sc[k];
+    int x = (int)std::floor(g[0]), y = (int)std::floor(g[1]), z = (int)std::floor(g[2]);
+    double fx = g[0] - x, fy = g[1] - y, fz = g[2] - z;
+    double den = 0.0;
+    for (int c = 0; c < 8; ++c) {
+      int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+      double w = (cx ? fx : 1.0 - fx) * (cy ? fy : 1.0 - fy) * (cz ? fz : 1.0 - fz);
+      den += w * G.at64(x + cx, y + cy, z + cz, rho64);
+    }
+    tr *= 1.0 - std::max(0.0, den * inv_maxd);
+    if (tr < (double)G.rr) {
+      double q = std::max(0.05, 1.0 - tr);
+      if (n_rr) ++*n_rr;
+      if (rs.next() < q) return 0.0;
+      tr /= 1.0 - q;
+    }
+  }
+  return tr;
+}
+
+inline RayStream stream_for(uint64_t seed, int64_t ray) {
+  RayStream rs;
+  rs.k0 = (uint32_t)seed;
+  rs.k1 = (uint32_t)(seed >> 32);
+  rs.rlo = (uint32_t)ray;
+  rs.rhi = (uint32_t)((uint64_t)ray >> 32);
+  return rs;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI of the oracle (loaded with ctypes by tests/ and bench.py).
+// ===========================================================================
+
+ORC_API int orc_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+ORC_API void orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+ORC_API void orc_philox(const uint32_t *ctr, const uint32_t *key, uint32_t *out) {
+  U4 r = philox(U4{ctr[0], ctr[1], ctr[2], ctr[3]}, key[0], key[1]);
+  out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
+}
+
+ORC_API void orc_logf(const float *x, float *y, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) y[i] = flg_logf(x[i]);
+}
+
+ORC_API void orc_stream_uniforms(uint64_t seed, int64_t ray, int32_t n, float *out) {
+  RayStream rs = stream_for(seed, ray);
+  for (int i = 0; i < n; ++i) out[i] = rs.next();
+}
+
+// prestage bounds reduce (radix_bvh.cpp:49-60): union of triangle AABBs.
+ORC_API void orc_scene_bound(const float *pos, const int32_t *idx, int64_t n_tri, float *out6) {
+  Mesh M{pos, idx, n_tri};
+  Bound b;
+#pragma omp parallel
+  {
+    Bound local;
+#pragma omp for schedule(static) nowait
+    for (int64_t i = 0; i < n_tri; ++i) local.merge(M.bound(i));
+#pragma omp critical
+    b.merge(local);
+  }
+  for (int k = 0; k < 3; ++k) {
+    out6[k] = b.lo[k];
+    out6[3 + k] = b.hi[k];
+  }
+}
+
+// prestage Morton loop (radix_bvh.cpp:63-73).
+ORC_API void orc_morton(const float *pos, const int32_t *idx, int64_t n_tri, const float *bound6,
+                        uint32_t *codes) {
+  Mesh M{pos, idx, n_tri};
+  Bound s;
+  for (int k = 0; k < 3; ++k) {
+    s.lo[k] = bound6[k];
+    s.hi[k] = bound6[3 + k];
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n_tri; ++i) codes[i] = morton_of(M.bound(i), s);
+}
+
+// Sort (radix_bvh.cpp:77-81) in the defined stable (code, index) order.
+ORC_API void orc_sort(const uint32_t *codes, int64_t n, uint32_t *sorted, int32_t *perm) {
+  std::vector<int32_t> p(n);
+  for (int64_t i = 0; i < n; ++i) p[i] = (int32_t)i;
+  std::stable_sort(p.begin(), p.end(), [&](int32_t a, int32_t b) { return codes[a] < codes[b]; });
+  for (int64_t i = 0; i < n; ++i) {
+    perm[i] = p[i];
+    sorted[i] = codes[p[i]];
+  }
+}
+
+// Karras node pass (radix_bvh.cpp:118-161).  parent: n-1 internal parents
+// (root keeps 0, as zero-initialised nodes do), leaf_parent: n.
+ORC_API void orc_karras(const uint32_t *sorted, int64_t n64, int32_t *split, uint8_t *leaf,
+                        int32_t *range_j, int32_t *parent, int32_t *leaf_parent) {
+  int n = (int)n64;
+  Karras K{sorted, n};
+  if (n >= 1) std::memset(parent, 0, sizeof(int32_t) * (size_t)std::max(n - 1, 0));
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n - 1; ++i) {
+    int dd = K.delta(i, i + 1) - K.delta(i, i - 1);
+    int d = dd == 0 ? 0 : (dd > 0 ? 1 : -1);
+    int delta_min = K.delta(i, i - d);
+    int l_max = 2;
+    while (K.delta(i, i + l_max * d) > delta_min) l_max <<= 1;
+    int l = 0;
+    for (int t = l_max / 2; t >= 1; t >>= 1)
+      if (K.delta(i, i + (l + t) * d) > delta_min) l += t;
+    int j = i + l * d;
+    int delta_node = K.delta(i, j);
+    int s = 0;
+    for (int t = next2pow(l); t >= 1; t >>= 1)
+      if (K.delta(i, i + (s + t) * d) > delta_node) s += t;
+    int sp = i + s * d + std::min(d, 0);
+    uint8_t lf = 0;
+    if (std::min(i, j) == sp) lf |= 1;
+    if (std::max(i, j) == sp + 1) lf |= 2;
+    split[i] = sp;
+    leaf[i] = lf;
+    range_j[i] = j;
+    if (lf & 1) leaf_parent[sp] = i; else parent[sp] = i;
+    if (lf & 2) leaf_parent[sp + 1] = i; else parent[sp + 1] = i;
+  }
+  if (n == 1) leaf_parent[0] = -1;
+}
+
+// Bottom-up refit (radix_bvh.cpp:163-199): one climber per leaf; the first
+// arrival at a node stops, the second merges the sibling bound and climbs on.
+// The reference's relaxed __sync_fetch_and_add is given acquire/release order
+// here so the sibling's bound is visible to the second arrival.
+ORC_API void orc_refit(const float *pos, const int32_t *idx, int64_t n64, const int32_t *perm,
+                       const int32_t *split, const uint8_t *leaf, const int32_t *parent,
+                       const int32_t *leaf_parent, float *nb) {
+  int n = (int)n64;
+  if (n < 2) return;
+  Mesh M{pos, idx, n64};
+  std::vector<std::atomic<int>> flag(n - 1);
+  for (auto &f : flag) f.store(0, std::memory_order_relaxed);
+  std::vector<Bound> bound(n - 1);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; ++i) {
+    int cur = leaf_parent[i];
+    int prev = i;
+    Bound sub = M.bound(perm[i]);
+    while (true) {
+      // The first arrival stops; its bound is re-read from the tree (leaf) or
+      // from bound[] (internal, published before its flag increment).
+      int pf = flag[cur].fetch_add(1, std::memory_order_acq_rel);
+      if (pf == 0) break;
+      int sp = split[cur];
+      uint8_t lf = leaf[cur];
+      Bound other;
+      if (prev == sp) {  // arrived from the left child (radix_bvh.cpp:177)
+        other = (lf & 2) ? M.bound(perm[sp + 1]) : bound[sp + 1];
+      } else {
+        other = (lf & 1) ? M.bound(perm[sp]) : bound[sp];
+      }
+      Bound nbd;
+      nbd.merge(other);
+      nbd.merge(sub);
+      bound[cur] = nbd;
+      std::atomic_thread_fence(std::memory_order_release);
+      sub = nbd;
+      if (cur == 0) break;
+      prev = cur;
+      cur = parent[cur];
+    }
+  }
+  for (int i = 0; i < n - 1; ++i)
+    for (int k = 0; k < 3; ++k) {
+      nb[6 * i + k] = bound[i].lo[k];
+      nb[6 * i + 3 + k] = bound[i].hi[k];
+    }
+}
+
+// Closest hit over a tree built by the functions above (recursiveIntersect).
+// rays: 8 SoA arrays of n floats (ox oy oz dx dy dz tmin tmax).  out: prim
+// (-1 = miss), t, u, v.
+ORC_API void orc_trace_closest(const float *pos, const int32_t *idx, int64_t n_tri,
+                               const int32_t *perm, const int32_t *split, const uint8_t *leaf,
+                               const float *nb, const float *rays, int64_t n, int32_t mode,
+                               int32_t *prim, float *t, float *u, float *v) {
+  Mesh M{pos, idx, n_tri};
+  Tree T{n_tri, perm, split, leaf, nb};
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    RayIn r = make_ray(rays, i, n);
+    Best b{r.tmax, -1, 0.0f, 0.0f};
+    if (n_tri == 1) {
+      Hit h;
+      if (pluecker(ld3(M.v(0, 0)), ld3(M.v(0, 1)), ld3(M.v(0, 2)), ld3(r.o), ld3(r.d), mode, &h) &&
+          !(h.t > b.tfar) && !(h.t < r.tmin))
+        b = Best{h.t, 0, h.u, h.v};
+    } else if (n_tri > 1) {
+      recursive_intersect(T, M, 0, r, mode, b);
+    }
+    prim[i] = b.prim;
+    t[i] = b.prim >= 0 ? b.tfar : r.tmax;
+    u[i] = b.u;
+    v[i] = b.v;
+  }
+}
+
+ORC_API void orc_trace_any(const float *pos, const int32_t *idx, int64_t n_tri, const int32_t *perm,
+                           const int32_t *split, const uint8_t *leaf, const float *nb,
+                           const float *rays, int64_t n, int32_t mode, uint8_t *occluded) {
+  Mesh M{pos, idx, n_tri};
+  Tree T{n_tri, perm, split, leaf, nb};
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    RayIn r = make_ray(rays, i, n);
+    bool occ = false;
+    if (n_tri == 1) {
+      Hit h;
+      occ = pluecker(ld3(M.v(0, 0)), ld3(M.v(0, 1)), ld3(M.v(0, 2)), ld3(r.o), ld3(r.d), mode, &h) &&
+            !(h.t > r.tmax) && !(h.t < r.tmin);
+    } else if (n_tri > 1) {
+      occ = recursive_occluded(T, M, 0, r, mode);
+    }
+    occluded[i] = occ ? 1 : 0;
+  }
+}
+
+// Single ray/triangle evaluation (tests use it to classify ties): returns 1 on
+// a hit and fills t, u, v.
+ORC_API int orc_pluecker(const float *a, const float *b, const float *c, const float *o,
+                         const float *d, int32_t mode, float *tuv) {
+  Hit h;
+  if (!pluecker(ld3(a), ld3(b), ld3(c), ld3(o), ld3(d), mode, &h)) return 0;
+  tuv[0] = h.t; tuv[1] = h.u; tuv[2] = h.v;
+  return 1;
+}
+
+// FP64 t, u, v of ray i against original triangle prim[i] (the FP64 oracle
+// for the GPU's hit values).  ok[i] = 0 where the triangle's plane is parallel.
+ORC_API void orc_hit_values64(const float *pos, const int32_t *idx, int64_t n_tri, const float *rays,
+                              int64_t n, const int32_t *prim, double *tuv, uint8_t *ok) {
+  Mesh M{pos, idx, n_tri};
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    ok[i] = 0;
+    tuv[3 * i] = tuv[3 * i + 1] = tuv[3 * i + 2] = 0.0;
+    if (prim[i] < 0) continue;
+    double O[3], D[3];
+    for (int k = 0; k < 3; ++k) {
+      O[k] = rays[k * n + i];
+      D[k] = rays[(3 + k) * n + i];
+    }
+    double t, u, v;
+    if (pluecker64(M.v(prim[i], 0), M.v(prim[i], 1), M.v(prim[i], 2), O, D, &t, &u, &v)) {
+      tuv[3 * i] = t; tuv[3 * i + 1] = u; tuv[3 * i + 2] = v;
+      ok[i] = 1;
+    }
+  }
+}
+
+// Gradient of (t, u, v) of a fixed hit with respect to the three vertices, in
+// FP64: with b = (1-u-v, u, v) and M = [D, -(p1-p0), -(p2-p0)],
+// dL/dp_k = b_k * M^{-T} (dL/dt, dL/du, dL/dv).  Accumulates into grad
+// (3 floats per vertex, or per soup corner).
+ORC_API void orc_hit_adjoint64(const float *pos, const int32_t *idx, int64_t n_tri, int64_t n_vert,
+                               const float *rays, int64_t n, const int32_t *prim, const float *g_t,
+                               const float *g_u, const float *g_v, double *grad) {
+  Mesh M{pos, idx, n_tri};
+  (void)n_vert;
+  for (int64_t i = 0; i < n; ++i) {
+    if (prim[i] < 0) continue;
+    double O[3], D[3];
+    for (int k = 0; k < 3; ++k) {
+      O[k] = rays[k * n + i];
+      D[k] = rays[(3 + k) * n + i];
+    }
+    const float *p[3] = {M.v(prim[i], 0), M.v(prim[i], 1), M.v(prim[i], 2)};
+    double t, u, v;
+    if (!pluecker64(p[0], p[1], p[2], O, D, &t, &u, &v)) continue;
+    double c1[3], c2[3], c3[3];
+    for (int k = 0; k < 3; ++k) {
+      c1[k] = D[k];
+      c2[k] = -((double)p[1][k] - p[0][k]);
+      c3[k] = -((double)p[2][k] - p[0][k]);
+    }
+    auto crs = [](const double *a, const double *b, double *r) {
+      r[0] = a[1] * b[2] - a[2] * b[1];
+      r[1] = a[2] * b[0] - a[0] * b[2];
+      r[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    double x23[3], x31[3], x12[3];
+    crs(c2, c3, x23); crs(c3, c1, x31); crs(c1, c2, x12);
+    double det = c1[0] * x23[0] + c1[1] * x23[1] + c1[2] * x23[2];
+    if (det == 0.0) continue;
+    double w[3];
+    for (int k = 0; k < 3; ++k) w[k] = (x23[k] * g_t[i] + x31[k] * g_u[i] + x12[k] * g_v[i]) / det;
+    double bc[3] = {1.0 - u - v, u, v};
+    for (int c = 0; c < 3; ++c) {
+      int64_t vi = idx ? (int64_t)idx[3 * prim[i] + c] : 3 * (int64_t)prim[i] + c;
+      for (int k = 0; k < 3; ++k) grad[3 * vi + k] += bc[c] * w[k];
+    }
+  }
+}
+
+// ------------------------------- volumes -----------------------------------
+
+struct OrcMedium {
+  float sigma_s, sigma_a, g, rr_threshold, majorant;
+};
+
+static Grid make_grid(const float *rho, int nx, int ny, int nz, const float *lo, const float *hi,
+                      const OrcMedium *m) {
+  Grid G;
+  G.rho = rho;
+  G.nx = nx; G.ny = ny; G.nz = nz;
+  int dims[3] = {nx, ny, nz};
+  for (int k = 0; k < 3; ++k) {
+    G.lo[k] = lo[k];
+    G.hi[k] = hi[k];
+    G.scale[k] = (float)(dims[k] - 1) / (hi[k] - lo[k]);
+  }
+  G.sigma_s = m->sigma_s;
+  G.sigma_a = m->sigma_a;
+  G.sigma_t = m->sigma_a + m->sigma_s;  // volume.cpp:38
+  G.g = m->g;
+  G.rr = m->rr_threshold;
+  float mx = m->majorant;
+  if (!(mx > 0.0f)) {
+    mx = 0.0f;
+    int64_t nv = (int64_t)nx * ny * nz;
+    for (int64_t i = 0; i < nv; ++i) mx = std::max(mx, rho[i]);
+  }
+  G.maxd = mx;
+  G.inv_maxd = (float)(1.0 / (double)mx);  // volume.cpp:55 (double quotient stored as Float)
+  return G;
+}
+
+ORC_API float orc_grid_majorant(const float *rho, int64_t nv) {
+  float mx = 0.0f;
+  for (int64_t i = 0; i < nv; ++i) mx = std::max(mx, rho[i]);
+  return mx;
+}
+
+// Ratio-tracking transmittance (fp32, same arithmetic as the GPU).  ck (may
+// be null): 3 arrays of n (t, k as float bits, c) = state after the last
+// Russian-roulette survival.
+ORC_API void orc_volume_tr(const float *rho, int nx, int ny, int nz, const float *lo, const float *hi,
+                           const OrcMedium *m, const float *rays, int64_t n, uint64_t seed,
+                           float *T, float *ck_t, uint32_t *ck_k, float *ck_c) {
+  Grid G = make_grid(rho, nx, ny, nz, lo, hi, m);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t i = 0; i < n; ++i) {
+    float o[3] = {rays[i], rays[n + i], rays[2 * n + i]};
+    float d[3] = {rays[3 * n + i], rays[4 * n + i], rays[5 * n + i]};
+    float tmax = rays[7 * n + i];
+    RayStream rs = stream_for(seed, i);
+    TrState ck;
+    T[i] = ratio_track(G, o, d, tmax, rs, &ck);
+    if (ck_t) { ck_t[i] = ck.t; ck_k[i] = ck.k; ck_c[i] = ck.c; }
+  }
+}
+
+// FP64 ratio tracking; rho64 (nullable) replaces the grid values so that tests
+// can take central finite differences.  n_rr (nullable) counts roulette events
+// per ray (used to exclude rays whose control flow flips between +h and -h).
+ORC_API void orc_volume_tr64(const float *rho, const double *rho64, int nx, int ny, int nz,
+                             const float *lo, const float *hi, const OrcMedium *m, const float *rays,
+                             int64_t n, uint64_t seed, double *T, int32_t *n_rr) {
+  Grid G = make_grid(rho, nx, ny, nz, lo, hi, m);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t i = 0; i < n; ++i) {
+    float o[3] = {rays[i], rays[n + i], rays[2 * n + i]};
+    float d[3] = {rays[3 * n + i], rays[4 * n + i], rays[5 * n + i]};
+    RayStream rs = stream_for(seed, i);
+    int nr = 0;
+    T[i] = ratio_track64(G, rho64, o, d, rays[7 * n + i], rs, &nr);
+    if (n_rr) n_rr[i] = nr;
+  }
+}
+
+// Adjoint of ratio tracking with respect to the grid, fp32 forward arithmetic
+// (identical to the GPU's) and FP64 accumulation:
+//   T = c * prod_{i in last segment} (1 - d_i / rho_max),
+//   dT/drho_v = sum_i -T / (1 - d_i/rho_max) * w_iv / rho_max,
+// with the majorant held constant (steps do not move with the grid) and the
+// roulette rescale 1/(1-q) = 1/T contributing nothing (T is reset to ~1).
+ORC_API void orc_volume_tr_adjoint(const float *rho, int nx, int ny, int nz, const float *lo,
+                                   const float *hi, const OrcMedium *m, const float *rays, int64_t n,
+                                   uint64_t seed, const float *dLdT, double *grad) {
+  Grid G = make_grid(rho, nx, ny, nz, lo, hi, m);
+  for (int64_t i = 0; i < n; ++i) {
+    float o[3] = {rays[i], rays[n + i], rays[2 * n + i]};
+    float d[3] = {rays[3 * n + i], rays[4 * n + i], rays[5 * n + i]};
+    float tmax = rays[7 * n + i];
+    RayStream rs = stream_for(seed, i);
+    TrState ck;
+    float Tf = ratio_track(G, o, d, tmax, rs, &ck);
+    if (Tf == 0.0f || dLdT[i] == 0.0f) continue;
+    float t_min, t_max;
+    if (!box_intersect_pbrt(G, o, d, tmax, &t_min, &t_max)) continue;
+    t_max = std::min(t_max, tmax);
+    float max_mu = G.sigma_t * G.maxd;
+    RayStream r2 = stream_for(seed, i);
+    r2.k = ck.k;
+    float t = ck.t;
+    for (int step_ = 0; step_ < kMaxTrackSteps; ++step_) {
+      float u = r2.next();
+      t += -flg_logf(1.0f - u) / max_mu;
+      if (t >= t_max) break;
+      float pos[3] = {o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t};
+      int b[3];
+      float f[3];
+      float den = G.sample(pos, b, f);
+      float x = den * G.inv_maxd;
+      if (!(x > 0.0f)) continue;
+      double fac = 1.0 - (double)x;
+      double coef = -(double)dLdT[i] * (double)Tf * (double)G.inv_maxd / fac;
+      for (int c = 0; c < 8; ++c) {
+        int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+        int X = b[0] + cx, Y = b[1] + cy, Z = b[2] + cz;
+        if (X < 0 || Y < 0 || Z < 0 || X >= nx || Y >= ny || Z >= nz) continue;
+        double w = (cx ? (double)f[0] : 1.0 - f[0]) * (cy ? (double)f[1] : 1.0 - f[1]) *
+                   (cz ? (double)f[2] : 1.0 - f[2]);
+        grad[((int64_t)Z * ny + Y) * nx + X] += coef * w;
+      }
+    }
+  }
+}
+
+// Delta tracking (OpenVDBVolume::sample, volume.cpp:109-148).  Outputs
+// success (0/1), collision position and the returned weight sigma_s/sigma_t
+// (1 when no collision).
+ORC_API void orc_volume_sample(const float *rho, int nx, int ny, int nz, const float *lo,
+                               const float *hi, const OrcMedium *m, const float *rays, int64_t n,
+                               uint64_t seed, uint8_t *success, float *p, float *weight) {
+  Grid G = make_grid(rho, nx, ny, nz, lo, hi, m);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int64_t i = 0; i < n; ++i) {
+    float o[3] = {rays[i], rays[n + i], rays[2 * n + i]};
+    float d[3] = {rays[3 * n + i], rays[4 * n + i], rays[5 * n + i]};
+    float tmax = rays[7 * n + i];
+    RayStream rs = stream_for(seed, i);
+    success[i] = 0;
+    weight[i] = 1.0f;
+    p[3 * i] = p[3 * i + 1] = p[3 * i + 2] = 0.0f;
+    float t_min, t_max;
+    if (!box_intersect_pbrt(G, o, d, tmax, &t_min, &t_max)) continue;
+    float t = std::max(t_min, 0.0f);
+    float max_mu = G.sigma_t * G.maxd;
+    t_max = std::min(t_max, tmax);
+    for (int step_ = 0; step_ < kMaxTrackSteps; ++step_) {
+      float u = rs.next();
+      t += -flg_logf(1.0f - u) / max_mu;
+      if (t >= t_max) break;
+      float pos[3] = {o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t};
+      int b[3];
+      float f[3];
+      float density = G.sample(pos, b, f);
+      float p_s = G.sigma_s * density / max_mu;
+      float p_a = G.sigma_a * density / max_mu;
+      float p_n = 1.0f - p_s - p_a;
+      if (rs.next() > p_n) {
+        success[i] = 1;
+        p[3 * i] = pos[0]; p[3 * i + 1] = pos[1]; p[3 * i + 2] = pos[2];
+        weight[i] = G.sigma_s / G.sigma_t;
+        break;
+      }
+    }
+  }
+}
+
+// Henyey-Greenstein phase function value (math_utils.h:103-107) — used by the
+// delta-tracking caller; exposed for tests.
+ORC_API float orc_hg_p(const float *wi, const float *wo, float g) {
+  float cos_theta = wi[0] * wo[0] + wi[1] * wo[1] + wi[2] * wo[2];
+  float denom = 1.0f + g * g + 2.0f * g * cos_theta;
+  return (1.0f - g * g) / (denom * std::sqrt(denom)) * 0.07957747154594766788f;
+}
+
+// ------------------------ reference-performance mode ------------------------
+// Build timed the way the reference runs it: parallel bounds reduce, parallel
+// Morton, parallel sort of 32-byte records (the RadixTriangle layout,
+// radix_bvh.hpp:35-37), parallel Karras and atomic refit.  Returns the node
+// count; outputs are the same arrays as the step-by-step functions.
+namespace {
+struct Rec32 {
+  const int32_t *v;
+  const void *mesh;
+  uint32_t code, parent;
+};
+}  // namespace
+
+ORC_API int64_t orc_build(const float *pos, const int32_t *idx, int64_t n_tri, uint32_t *sorted,
+                          int32_t *perm, int32_t *split, uint8_t *leaf, int32_t *range_j,
+                          int32_t *parent, int32_t *leaf_parent, float *nb) {
+  if (n_tri <= 0) return 0;
+  float b6[6];
+  orc_scene_bound(pos, idx, n_tri, b6);
+  std::vector<uint32_t> codes(n_tri);
+  orc_morton(pos, idx, n_tri, b6, codes.data());
+  std::vector<Rec32> rec(n_tri);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n_tri; ++i) rec[i] = Rec32{idx ? idx + 3 * i : nullptr, (const void *)(intptr_t)i, codes[i], 0};
+  __gnu_parallel::stable_sort(rec.begin(), rec.end(),
+                              [](const Rec32 &a, const Rec32 &b) { return a.code < b.code; });
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n_tri; ++i) {
+    sorted[i] = rec[i].code;
+    perm[i] = (int32_t)(intptr_t)rec[i].mesh;
+  }
+  orc_karras(sorted, n_tri, split, leaf, range_j, parent, leaf_parent);
+  orc_refit(pos, idx, n_tri, perm, split, leaf, parent, leaf_parent, nb);
+  return n_tri - 1;
+}

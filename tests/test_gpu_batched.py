@@ -1,0 +1,128 @@
+"""Batched scenes (one segmented build, one persistent trace), CUDA-graph
+replay, and the error paths of the C ABI on the GPU."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+import geometry as G
+import gpu_util as U
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(ctx, counts, rays_per_tri=8, seed=3, width=4):
+    import fledge_gb300 as F
+    offs = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    roffs = offs * rays_per_tri
+    pos = F.gen_triangles(ctx, int(offs[-1]), seed)
+    soa = F.gen_rays(ctx, int(roffs[-1]), seed + 1)
+    bb = F.BatchedRadixBVHBuilder(F.InternalTriangleMesh(pos), offs, ctx, node_width=width)
+    bb.build()
+    return bb, pos, soa, offs, roffs
+
+
+@pytest.mark.parametrize("opts", [{}, {"persistent": 1, "refill_lanes": 16}, {"persistent": 1, "refill_lanes": 1}])
+def test_batched_trace_equals_per_scene(ctx, oracle, opts):
+    import fledge_gb300 as F
+    counts = [1, 2, 1000, 37, 20000, 5, 3000]
+    bb, pos, soa, offs, roffs = _batch(ctx, counts)
+    rays = F.Rays.from_soa(soa, tmin=1e-4)
+    hb = U.host(bb.intersect_batched(rays, roffs, **opts))
+    ph, rh = pos.cpu().numpy(), soa.cpu().numpy()
+    for s in range(len(counts)):
+        sp = ph[3 * offs[s]:3 * offs[s + 1]]
+        r8 = np.zeros((8, roffs[s + 1] - roffs[s]), np.float32)
+        r8[:6] = rh[:, roffs[s]:roffs[s + 1]]
+        r8[6], r8[7] = np.float32(1e-4), np.inf
+        tree = oracle.build_bvh(sp)
+        hs = {k: v[roffs[s]:roffs[s + 1]] for k, v in hb.items()}
+        bad, ties, _ = U.compare_closest(oracle, sp, None, tree, r8, hs, oracle.MODE_DEV)
+        assert bad == 0, (s, bad)
+
+
+def test_batched_persistent_equals_plain(ctx):
+    import fledge_gb300 as F
+    rng = np.random.default_rng(8)
+    counts = np.round(np.exp(rng.uniform(np.log(1e3), np.log(1e5), 24))).astype(np.int64)
+    bb, pos, soa, offs, roffs = _batch(ctx, counts, rays_per_tri=4)
+    rays = F.Rays.from_soa(soa, tmin=1e-4)
+    a = U.host(bb.intersect_batched(rays, roffs))
+    b = U.host(bb.intersect_batched(rays, roffs, persistent=1, refill_lanes=12))
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_graph_capture_rebuild_and_trace(ctx, oracle):
+    """Build + trace captured once, replayed after the vertices change in place."""
+    import fledge_gb300 as F
+    n = 50000
+    pos = F.gen_triangles(ctx, n, 5)
+    soa = F.gen_rays(ctx, 1 << 18, 6)
+    b = F.RadixBVHBuilder(F.InternalTriangleMesh(pos), ctx, node_width=4)
+    b.build()
+    rays = F.Rays.from_soa(soa, tmin=1e-4)
+    out = b.intersect(rays)  # allocates scratch before capture
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    ctx2 = F.Context(0, s)
+    g = C.c_void_p()
+    r0, h0, op0 = rays.struct(), F._hits_struct(out), F.FlgTraceOpts()
+    # first trace on a context allocates its scratch: do it before capturing
+    ctx2.check(ctx2.lib.flg_trace_closest(ctx2.h, b.h, C.byref(r0), rays.n, C.byref(op0), C.byref(h0)))
+    ctx2.sync()
+    with torch.cuda.stream(s):
+        ctx2.check(ctx2.lib.flg_graph_begin(ctx2.h))
+        ctx2.check(ctx2.lib.flg_bvh_rebuild(ctx2.h, b.h, C.c_void_p(pos.data_ptr())))
+        r, hs, op = rays.struct(), F._hits_struct(out), F.FlgTraceOpts()
+        ctx2.check(ctx2.lib.flg_trace_closest(ctx2.h, b.h, C.byref(r), rays.n, C.byref(op), C.byref(hs)))
+        ctx2.check(ctx2.lib.flg_graph_end(ctx2.h, C.byref(g)))
+    for trial in range(2):
+        pos.copy_(F.gen_triangles(ctx, n, 100 + trial))
+        torch.cuda.synchronize()
+        ctx2.check(ctx2.lib.flg_graph_launch(ctx2.h, g))
+        ctx2.sync()
+        ph = pos.cpu().numpy()
+        r8 = np.zeros((8, rays.n), np.float32)
+        r8[:6] = soa.cpu().numpy()
+        r8[6], r8[7] = np.float32(1e-4), np.inf
+        tree = oracle.build_bvh(ph)
+        bad, _, _ = U.compare_closest(oracle, ph, None, tree, r8, U.host(out), oracle.MODE_DEV)
+        assert bad == 0
+    ctx2.lib.flg_graph_destroy(g)
+    ctx2.close()
+
+
+def test_bounded_wait_times_out_and_context_survives(ctx):
+    """A wait on a device flag that nothing sets returns FLG_ERR_TIMEOUT after
+    its poll limit; the context keeps working afterwards."""
+    from fledge_gb300 import _lib
+    assert ctx.lib.flg_debug_wait_unset_flag(ctx.h, 2000) == _lib.FLG_ERR_TIMEOUT
+    assert ctx.lib.flg_ctx_sync(ctx.h) == _lib.FLG_OK
+    pos = G.random_soup(1000, np.random.default_rng(1))
+    b, _ = U.gpu_build(ctx, pos)
+    ctx.sync()
+
+
+def test_argument_errors_launch_nothing(ctx):
+    import fledge_gb300 as F
+    from fledge_gb300 import _lib
+    h = C.c_void_p()
+    opts = F.FlgBuildOpts(3, 1, 1)
+    p = torch.zeros((30, 3), device="cuda")
+    assert ctx.lib.flg_bvh_build(ctx.h, C.c_void_p(p.data_ptr()), None, 10, 30, C.byref(opts),
+                                 C.byref(h)) == _lib.FLG_ERR_ARG
+    opts = F.FlgBuildOpts(4, 1, 1)
+    assert ctx.lib.flg_bvh_build(ctx.h, C.c_void_p(p.data_ptr()), None, 10, 29, C.byref(opts),
+                                 C.byref(h)) == _lib.FLG_ERR_ARG
+    assert ctx.lib.flg_bvh_build(ctx.h, None, None, 10, 30, C.byref(opts), C.byref(h)) == _lib.FLG_ERR_ARG
+    offs = (C.c_int64 * 3)(0, 5, 3)
+    assert ctx.lib.flg_bvh_build_batched(ctx.h, C.c_void_p(p.data_ptr()), None, offs, 2, 15, C.byref(opts),
+                                         C.byref(h)) == _lib.FLG_ERR_ARG
+    b, _ = U.gpu_build(ctx, G.random_soup(10, np.random.default_rng(0)))
+    r = F.FlgRays()
+    hs = F.FlgHits()
+    op = F.FlgTraceOpts(48, 0, 0, 0, 0)
+    assert ctx.lib.flg_trace_closest(ctx.h, b.h, C.byref(r), 5, C.byref(op), C.byref(hs)) == _lib.FLG_ERR_ARG
+    ctx.sync()
