@@ -44,9 +44,20 @@ BYTES_PER_RAY = 24 + 16
 BYTES_PER_TRI_BATCHED = 36 + 44 + (4 + 5 * 24) + 20 + 100
 
 
-def scene_counts(seed: int = SEED_C3, n: int = N_SCENES) -> np.ndarray:
+_T0 = time.perf_counter()
+_VERBOSE = False
+
+
+def log(msg: str) -> None:
+    if _VERBOSE:
+        sys.stderr.write(f"[bench {time.perf_counter() - _T0:8.2f}s] {msg}\n")
+        sys.stderr.flush()
+
+
+def scene_counts(seed: int = SEED_C3, n: int = None) -> np.ndarray:
     rng = np.random.default_rng(seed)
-    return np.round(np.exp(rng.uniform(math.log(1e3), math.log(1e6), n))).astype(np.int64)
+    c = np.round(np.exp(rng.uniform(math.log(1e3), math.log(1e6), N_SCENES))).astype(np.int64)
+    return c if n is None else c[:n]
 
 
 def peaks() -> dict:
@@ -194,6 +205,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     offs = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
     roffs = offs * RAYS_PER_TRI
     n_tri, n_rays = int(offs[-1]), int(roffs[-1])
+    log(f'generating {n_tri} triangles, {n_rays} rays')
     pos = F.gen_triangles(ctx, n_tri, SEED_C3)
     soa = torch.empty((6, n_rays), dtype=torch.float32, device=dev)
     chunk = 1 << 28
@@ -210,6 +222,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     mesh = F.InternalTriangleMesh(pos)
     width, leaf = args.width, args.leaf
     bb = F.BatchedRadixBVHBuilder(mesh, offs, ctx, node_width=width, leaf_size=leaf)
+    log('first build')
     bb.build()
     topts = dict(persistent=1, refill_lanes=args.refill, stack_depth=64)
     ctx.sync()
@@ -226,11 +239,13 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         if ev:
             ev[2].record(stream)
 
+    log('warm-up steps')
     for _ in range(args.warmup):
         step()
     ctx.sync()
     barrier()
     torch.cuda.synchronize()
+    log('timed steps')
     clk = ClockSampler(local_rank)
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
     l0 = lib.flg_ctx_launch_count(ctx.h)
@@ -268,6 +283,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                   "bytes_per_tri": BYTES_PER_TRI_BATCHED}
 
     # ---- plain path: one build + one trace launch per scene (BVH2 kernel) ----
+    log(f'timed: {total_ms / args.steps:.1f} ms/step, build {statistics.median(build_ms):.2f} ms')
     plain = None
     if not args.skip_plain:
         handles = []
@@ -300,14 +316,17 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         del handles
 
     # ---- e2e: host (pinned) inputs, copies inside the timed region ----
+    log('plain path done' if plain else 'plain skipped')
     e2e = None
     if not args.skip_e2e:
         e2e = run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, leaf, topts, dev, world)
 
     # ---- volume: config 2 forward + adjoint ----
+    log('e2e done')
     vol = run_volume(ctx, torch, F, dev) if not args.skip_volume else None
 
     # ---- CPU baseline (rank 0) ----
+    log('volume done')
     cpu = None
     if rank == 0 and not args.skip_cpu:
         from oracle import oracle as O
@@ -468,7 +487,12 @@ def main() -> None:
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-volume", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--scenes", type=int, default=256, help="diagnostics only: first N scenes")
+    ap.add_argument("--verbose", action="store_true", help="progress on stderr")
     args = ap.parse_args()
+    global N_SCENES, _VERBOSE
+    N_SCENES = args.scenes
+    _VERBOSE = args.verbose
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

@@ -130,7 +130,8 @@ struct Box {
 // --------------------------------------------------------------------------
 // Slab test (BoundIntersect, intersector.hpp:103-120): t0 starts at 0 and t1
 // at FLT_MAX; a NaN slab (0 * inf) leaves the interval unchanged, as the
-// reference's compare-and-swap does.  Returns tnear, or +inf on a miss.
+// reference's compare-and-swap does.  Returns tnear, or NaN on a miss (so
+// that `t <= limit` is false on a miss even when the limit is +inf).
 // --------------------------------------------------------------------------
 __device__ __forceinline__ float slab1(float lo, float hi, float o, float inv, float &t0, float &t1) {
   float tn = (lo - o) * inv;
@@ -149,7 +150,7 @@ __device__ __forceinline__ float slab_tnear(float lox, float hix, float loy, flo
   slab1(lox, hix, o.x, inv.x, t0, t1);
   slab1(loy, hiy, o.y, inv.y, t0, t1);
   slab1(loz, hiz, o.z, inv.z, t0, t1);
-  return t0 > t1 ? __int_as_float(0x7f800000) : t0;
+  return t0 > t1 ? __int_as_float(0x7fffffff) : t0;
 }
 
 // --------------------------------------------------------------------------

@@ -136,7 +136,7 @@ __device__ __forceinline__ bool trace_bvh2(const Node2 *__restrict__ nodes, cons
   uint64_t stk[STACK];
   int sp = 0;
   int32_t cur = root;
-  const float inf = __int_as_float(0x7f800000);
+  const float miss = __int_as_float(0x7fffffff);  // NaN: never <= a limit
   while (true) {
     const float4 *np = (const float4 *)(nodes + cur);
     const float4 A = __ldg(np), B = __ldg(np + 1), C = __ldg(np + 2);
@@ -157,9 +157,9 @@ __device__ __forceinline__ bool trace_bvh2(const Node2 *__restrict__ nodes, cons
       }
     }
     const float lim = ANY ? tmax : best;
-    float t0 = c0 >= 0 ? slab_tnear(A.x, A.y, A.z, A.w, C.x, C.y, o, inv) : inf;
-    float t1 = c1 >= 0 ? slab_tnear(B.x, B.y, B.z, B.w, C.z, C.w, o, inv) : inf;
-    const bool h0 = t0 <= lim, h1 = t1 <= lim;
+    float t0 = c0 >= 0 ? slab_tnear(A.x, A.y, A.z, A.w, C.x, C.y, o, inv) : miss;
+    float t1 = c1 >= 0 ? slab_tnear(B.x, B.y, B.z, B.w, C.z, C.w, o, inv) : miss;
+    const bool h0 = c0 >= 0 && t0 <= lim, h1 = c1 >= 0 && t1 <= lim;
     if (h0 && h1) {
       if (sp >= STACK) return false;
       const bool swap = t1 < t0;
