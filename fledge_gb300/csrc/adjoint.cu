@@ -11,8 +11,8 @@
 
 namespace flg {
 
-__device__ __forceinline__ float3 crossf(float3 a, float3 b) {
-  return make_float3(fmaf(a.y, b.z, -a.z * b.y), fmaf(a.z, b.x, -a.x * b.z), fmaf(a.x, b.y, -a.y * b.x));
+__device__ __forceinline__ double3 crossd(double3 a, double3 b) {
+  return make_double3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 
 __global__ void __launch_bounds__(256)
@@ -29,26 +29,27 @@ __global__ void __launch_bounds__(256)
   if (g0 == 0.0f && g1 == 0.0f && g2 == 0.0f) return;
   int64_t vi[3];
   for (int k = 0; k < 3; ++k) vi[k] = idx ? (int64_t)idx[3 * (int64_t)p + k] : 3 * (int64_t)p + k;
-  const float3 p0 = make_float3(pos[3 * vi[0]], pos[3 * vi[0] + 1], pos[3 * vi[0] + 2]);
-  const float3 p1 = make_float3(pos[3 * vi[1]], pos[3 * vi[1] + 1], pos[3 * vi[1] + 2]);
-  const float3 p2 = make_float3(pos[3 * vi[2]], pos[3 * vi[2] + 1], pos[3 * vi[2] + 2]);
-  const float3 c1 = make_float3(dx[i], dy[i], dz[i]);
-  const float3 c2 = make_float3(p0.x - p1.x, p0.y - p1.y, p0.z - p1.z);
-  const float3 c3 = make_float3(p0.x - p2.x, p0.y - p2.y, p0.z - p2.z);
-  const float3 x23 = crossf(c2, c3), x31 = crossf(c3, c1), x12 = crossf(c1, c2);
-  const float det = fmaf(c1.x, x23.x, fmaf(c1.y, x23.y, c1.z * x23.z));
-  if (det == 0.0f) return;
-  const float r = 1.0f / det;
-  const float3 w = make_float3(fmaf(x23.x, g0, fmaf(x31.x, g1, x12.x * g2)) * r,
-                               fmaf(x23.y, g0, fmaf(x31.y, g1, x12.y * g2)) * r,
-                               fmaf(x23.z, g0, fmaf(x31.z, g1, x12.z * g2)) * r);
-  const float u = hu[i], v = hv[i];
-  const float b[3] = {1.0f - u - v, u, v};
+  // The 3x3 solve runs in double precision: for grazing rays det M is small
+  // and an fp32 solve loses the digits the 1e-3 gradient bar needs.  It is
+  // one solve per hit, negligible next to the traversal.
+  const double3 p0 = make_double3(pos[3 * vi[0]], pos[3 * vi[0] + 1], pos[3 * vi[0] + 2]);
+  const double3 p1 = make_double3(pos[3 * vi[1]], pos[3 * vi[1] + 1], pos[3 * vi[1] + 2]);
+  const double3 p2 = make_double3(pos[3 * vi[2]], pos[3 * vi[2] + 1], pos[3 * vi[2] + 2]);
+  const double3 c1 = make_double3(dx[i], dy[i], dz[i]);
+  const double3 c2 = make_double3(p0.x - p1.x, p0.y - p1.y, p0.z - p1.z);
+  const double3 c3 = make_double3(p0.x - p2.x, p0.y - p2.y, p0.z - p2.z);
+  const double3 x23 = crossd(c2, c3), x31 = crossd(c3, c1), x12 = crossd(c1, c2);
+  const double det = c1.x * x23.x + c1.y * x23.y + c1.z * x23.z;
+  if (det == 0.0) return;
+  const double w[3] = {(x23.x * g0 + x31.x * g1 + x12.x * g2) / det, (x23.y * g0 + x31.y * g1 + x12.y * g2) / det,
+                       (x23.z * g0 + x31.z * g1 + x12.z * g2) / det};
+  const double u = hu[i], v = hv[i];
+  const double b[3] = {1.0 - u - v, u, v};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    atomicAdd(grad + 3 * vi[k], b[k] * w.x);
-    atomicAdd(grad + 3 * vi[k] + 1, b[k] * w.y);
-    atomicAdd(grad + 3 * vi[k] + 2, b[k] * w.z);
+    atomicAdd(grad + 3 * vi[k], (float)(b[k] * w[0]));
+    atomicAdd(grad + 3 * vi[k] + 1, (float)(b[k] * w[1]));
+    atomicAdd(grad + 3 * vi[k] + 2, (float)(b[k] * w[2]));
   }
 }
 

@@ -207,6 +207,36 @@ __device__ __forceinline__ bool pluecker(float3 a, float3 b, float3 c, float3 O,
   return true;
 }
 
+// Hit values of the selected triangle recomputed in double precision (same
+// Pluecker quantities: t = (v0.N)/(N.D) with N = e0 x e1, u = U/S, v = V/S)
+// and rounded once to fp32.  The fp32 test above decides hit/miss and which
+// triangle is closest; this makes the reported t, u, v accurate to an ulp
+// even for grazing rays, where the fp32 quotient loses digits.  Leaves the
+// inputs unchanged when the double-precision plane is degenerate.
+__device__ __forceinline__ void refine_tuv(float3 a, float3 b, float3 c, float3 O, float3 D, float &t, float &u,
+                                           float &v) {
+  const double Ox = O.x, Oy = O.y, Oz = O.z, Dx = D.x, Dy = D.y, Dz = D.z;
+  const double v0x = (double)a.x - Ox, v0y = (double)a.y - Oy, v0z = (double)a.z - Oz;
+  const double v1x = (double)b.x - Ox, v1y = (double)b.y - Oy, v1z = (double)b.z - Oz;
+  const double v2x = (double)c.x - Ox, v2y = (double)c.y - Oy, v2z = (double)c.z - Oz;
+  const double e0x = v2x - v0x, e0y = v2y - v0y, e0z = v2z - v0z;
+  const double e1x = v0x - v1x, e1y = v0y - v1y, e1z = v0z - v1z;
+  const double e2x = v1x - v2x, e2y = v1y - v2y, e2z = v1z - v2z;
+  const double s0x = v2x + v0x, s0y = v2y + v0y, s0z = v2z + v0z;
+  const double s1x = v0x + v1x, s1y = v0y + v1y, s1z = v0z + v1z;
+  const double s2x = v1x + v2x, s2y = v1y + v2y, s2z = v1z + v2z;
+  const double U = (e0y * s0z - e0z * s0y) * Dx + (e0z * s0x - e0x * s0z) * Dy + (e0x * s0y - e0y * s0x) * Dz;
+  const double V = (e1y * s1z - e1z * s1y) * Dx + (e1z * s1x - e1x * s1z) * Dy + (e1x * s1y - e1y * s1x) * Dz;
+  const double W = (e2y * s2z - e2z * s2y) * Dx + (e2z * s2x - e2x * s2z) * Dy + (e2x * s2y - e2y * s2x) * Dz;
+  const double S = U + V + W;
+  const double Nx = e0y * e1z - e0z * e1y, Ny = e0z * e1x - e0x * e1z, Nz = e0x * e1y - e0y * e1x;
+  const double den = Nx * Dx + Ny * Dy + Nz * Dz;
+  if (den == 0.0 || S == 0.0) return;
+  t = (float)((v0x * Nx + v0y * Ny + v0z * Nz) / den);
+  u = (float)(U / S);
+  v = (float)(V / S);
+}
+
 // Accept a candidate t for closest hit: tmin <= t, and t < best (or t == best
 // when nothing has been accepted yet, so that t == tmax counts as in the
 // reference's `thit > tfar` rejection).

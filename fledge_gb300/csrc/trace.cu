@@ -75,7 +75,7 @@ __device__ __forceinline__ bool test_tri(const TriRec *__restrict__ tris, int64_
   if (!accept_closest(t, tmin, best, have)) return false;
   best = t;
   have = true;
-  prim = __float_as_int(a.w);
+  prim = (int32_t)g;  // sorted position; write_result maps it to the original id
   hu = u;
   hv = v;
   return true;
@@ -97,11 +97,22 @@ __device__ __forceinline__ uint64_t stack_key(float t, int32_t ref) {
   return ((uint64_t)(__float_as_uint(t) & 0x7FFFFFFFu) << 32) | (uint32_t)ref;
 }
 
+// Writes one ray's result.  For closest hit, `prim` holds the sorted
+// position of the winning triangle: its record gives the original id and the
+// vertices for the double-precision refinement of t, u, v.
 __device__ __forceinline__ void write_result(const Out &O, int64_t i, bool any, bool have, int32_t prim,
-                                             float best, float tmax, float u, float v) {
+                                             float best, float tmax, float u, float v,
+                                             const TriRec *__restrict__ tris, const float3 &o, const float3 &d) {
   if (any) {
     O.occ[i] = have ? 1 : 0;
   } else {
+    if (have) {
+      const float4 *p = (const float4 *)(tris + prim);
+      const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+      refine_tuv(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z), o, d, best,
+                 u, v);
+      prim = __float_as_int(a.w);
+    }
     O.prim[i] = have ? prim : -1;
     O.t[i] = have ? best : tmax;
     O.u[i] = have ? u : 0.0f;
@@ -198,7 +209,7 @@ __global__ void __launch_bounds__(256)
     record_overflow(S, i);
     return;
   }
-  write_result(O, i, ANY, have, prim, best, tmax, hu, hv);
+  write_result(O, i, ANY, have, prim, best, tmax, hu, hv, tris, o, d);
 }
 
 // ----------------------------------------------------------------------------
@@ -320,7 +331,7 @@ __global__ void __launch_bounds__(256)
   while (!tr.step(nodes, tris)) {
   }
   if (tr.overflow) record_overflow(S, i);
-  else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv);
+  else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv, tris, tr.o, tr.d);
 }
 
 template <int W, bool ANY, int STACK>
@@ -357,7 +368,7 @@ __global__ void __launch_bounds__(256)
     }
     if (active && tr.step(nodes, tris)) {
       if (tr.overflow) record_overflow(S, ray);
-      else write_result(O, ray, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv);
+      else write_result(O, ray, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv, tris, tr.o, tr.d);
       active = false;
     }
   }
@@ -384,7 +395,7 @@ __global__ void __launch_bounds__(128)
         atomicOr(S.err, kErrStack);
         continue;
       }
-      write_result(O, i, ANY, have, prim, best, tmax, hu, hv);
+      write_result(O, i, ANY, have, prim, best, tmax, hu, hv, tris, o, d);
     } else {
       Tracer<(W == 2 ? 4 : W), ANY, kRetryStack> tr;
       tr.o = o; tr.d = d; tr.inv = inv; tr.tmin = tmin; tr.tmax = tmax;
@@ -392,7 +403,7 @@ __global__ void __launch_bounds__(128)
       while (!tr.step(nodes, tris)) {
       }
       if (tr.overflow) atomicOr(S.err, kErrStack);
-      else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv);
+      else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv, tris, tr.o, tr.d);
     }
   }
 }
@@ -653,14 +664,18 @@ FLG_API int flg_autotune_trace(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, i
   const int orig_w = bvh->width, orig_leaf = bvh->leaf_size;
   bool first = true;
   for (int w : {2, 4, 8}) {
-    for (int leaf : (w == 2 ? std::initializer_list<int>{1} : std::initializer_list<int>{1, 2, 4})) {
+    static const int kLeaves[3] = {1, 2, 4};
+    for (int li = 0; li < (w == 2 ? 1 : 3); ++li) {
+      const int leaf = kLeaves[li];
       rc = flg_bvh_set_width(ctx, bvh, w, leaf);
       if (rc) goto done;
       for (int stack : {32, 64}) {
         if (w == 2 && stack == 32) continue;
         for (int pers : {0, 1}) {
           if (w == 2 && pers) continue;
-          for (int refill : (pers ? std::initializer_list<int>{8, 16, 24} : std::initializer_list<int>{0})) {
+          static const int kRefill[3] = {8, 16, 24};
+          for (int ri = 0; ri < (pers ? 3 : 1); ++ri) {
+            const int refill = pers ? kRefill[ri] : 0;
             for (int threads : {128, 256}) {
               flg_trace_opts op{};
               op.stack_depth = stack;

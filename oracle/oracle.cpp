@@ -736,6 +736,17 @@ ORC_API void orc_trace_closest(const float *pos, const int32_t *idx, int64_t n_t
     } else if (n_tri > 1) {
       recursive_intersect(T, M, 0, r, mode, b);
     }
+    if (mode == MODE_DEV && b.prim >= 0) {
+      // The GPU reports the selected triangle's t, u, v recomputed in double
+      // precision and rounded once (refine_tuv); same expression here.
+      double O[3] = {r.o[0], r.o[1], r.o[2]}, D[3] = {r.d[0], r.d[1], r.d[2]};
+      double t64, u64, v64;
+      if (pluecker64(M.v(b.prim, 0), M.v(b.prim, 1), M.v(b.prim, 2), O, D, &t64, &u64, &v64)) {
+        b.tfar = (float)t64;
+        b.u = (float)u64;
+        b.v = (float)v64;
+      }
+    }
     prim[i] = b.prim;
     t[i] = b.prim >= 0 ? b.tfar : r.tmax;
     u[i] = b.u;

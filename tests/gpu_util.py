@@ -57,8 +57,11 @@ def compare_closest(oracle, pos, ind, tree, r8, hg, mode, allow_rel=0.0):
         pg, po = hg["prim"][i], ho["prim"][i]
         if pg < 0 or po < 0:
             continue
+        # both triangles are hit, at the same fp32 distance of the test that
+        # selects the closest one (reported t values are refined afterwards)
         okg, tg = oracle.pluecker(tri[pg, 0], tri[pg, 1], tri[pg, 2], r8[0:3, i], r8[3:6, i], mode)
-        if okg and abs(float(tg[0]) - float(ho["t"][i])) <= allow_rel * abs(float(ho["t"][i])):
+        oko, to = oracle.pluecker(tri[po, 0], tri[po, 1], tri[po, 2], r8[0:3, i], r8[3:6, i], mode)
+        if okg and oko and abs(float(tg[0]) - float(to[0])) <= allow_rel * abs(float(to[0])):
             ties += 1
     return len(diff) - ties, ties, ho
 

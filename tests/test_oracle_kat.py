@@ -185,8 +185,11 @@ def test_bvh_agrees_with_bruteforce(oracle):
             if ok and tuv[0] < best:
                 best, bp = tuv[0], k
         assert h["prim"][i] == bp
-        if bp >= 0:
-            assert h["t"][i] == np.float32(best)
+    # reported t, u, v are the selected triangle's FP64 values rounded once
+    tuv, ok = oracle.hit_values64(pos, None, 300, rays, h["prim"])
+    hit = h["prim"] >= 0
+    assert np.array_equal(h["t"][hit], tuv[hit, 0].astype(np.float32))
+    assert np.array_equal(h["u"][hit], tuv[hit, 1].astype(np.float32))
 
 
 def test_any_hit_consistent_with_closest(oracle):
