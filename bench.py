@@ -224,7 +224,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     bb = F.BatchedRadixBVHBuilder(mesh, offs, ctx, node_width=width, leaf_size=leaf)
     log('first build')
     bb.build()
-    topts = dict(persistent=1, refill_lanes=args.refill, stack_depth=64)
+    topts = dict(persistent=args.persistent, refill_lanes=args.refill, stack_depth=args.stack)
     ctx.sync()
 
     stream = torch.cuda.current_stream(dev)
@@ -274,7 +274,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     trace_bytes = n_rays * BYTES_PER_RAY + int(bb.info().device_bytes)
     tr_ms = statistics.median(trace_ms)
     roof = {"bound": "hbm", "achieved": round(trace_bytes / (tr_ms * 1e-3) / 1e9, 1), "peak": pk["hbm_gbs"],
-            "unit": "GB/s", "frac": None, "traffic": None, "kernel": "k_trace_persistent<4,false,64>",
+            "unit": "GB/s", "frac": None, "traffic": None,
+            "kernel": (f"k_trace_persistent<{width},false,{args.stack}>" if args.persistent and width > 2
+                       else f"k_trace_wide<{width},false,{args.stack}>" if width > 2 else "k_trace_bvh2<false>"),
             "peak_source": pk["source"]}
     roof["frac"] = round(roof["achieved"] / roof["peak"], 4)
     b_ms = statistics.median(build_ms)
@@ -482,6 +484,8 @@ def main() -> None:
     ap.add_argument("--width", type=int, default=4)
     ap.add_argument("--leaf", type=int, default=1)
     ap.add_argument("--refill", type=int, default=16)
+    ap.add_argument("--persistent", type=int, default=1)
+    ap.add_argument("--stack", type=int, default=64)
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")

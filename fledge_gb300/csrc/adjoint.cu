@@ -11,8 +11,10 @@
 
 namespace flg {
 
-__device__ __forceinline__ double3 crossd(double3 a, double3 b) {
-  return make_double3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+__device__ __forceinline__ void crossdf(const dfl *a, const dfl *b, dfl *r) {
+  r[0] = df_sub(df_mul(a[1], b[2]), df_mul(a[2], b[1]));
+  r[1] = df_sub(df_mul(a[2], b[0]), df_mul(a[0], b[2]));
+  r[2] = df_sub(df_mul(a[0], b[1]), df_mul(a[1], b[0]));
 }
 
 __global__ void __launch_bounds__(256)
@@ -29,27 +31,37 @@ __global__ void __launch_bounds__(256)
   if (g0 == 0.0f && g1 == 0.0f && g2 == 0.0f) return;
   int64_t vi[3];
   for (int k = 0; k < 3; ++k) vi[k] = idx ? (int64_t)idx[3 * (int64_t)p + k] : 3 * (int64_t)p + k;
-  // The 3x3 solve runs in double precision: for grazing rays det M is small
-  // and an fp32 solve loses the digits the 1e-3 gradient bar needs.  It is
-  // one solve per hit, negligible next to the traversal.
-  const double3 p0 = make_double3(pos[3 * vi[0]], pos[3 * vi[0] + 1], pos[3 * vi[0] + 2]);
-  const double3 p1 = make_double3(pos[3 * vi[1]], pos[3 * vi[1] + 1], pos[3 * vi[1] + 2]);
-  const double3 p2 = make_double3(pos[3 * vi[2]], pos[3 * vi[2] + 1], pos[3 * vi[2] + 2]);
-  const double3 c1 = make_double3(dx[i], dy[i], dz[i]);
-  const double3 c2 = make_double3(p0.x - p1.x, p0.y - p1.y, p0.z - p1.z);
-  const double3 c3 = make_double3(p0.x - p2.x, p0.y - p2.y, p0.z - p2.z);
-  const double3 x23 = crossd(c2, c3), x31 = crossd(c3, c1), x12 = crossd(c1, c2);
-  const double det = c1.x * x23.x + c1.y * x23.y + c1.z * x23.z;
-  if (det == 0.0) return;
-  const double w[3] = {(x23.x * g0 + x31.x * g1 + x12.x * g2) / det, (x23.y * g0 + x31.y * g1 + x12.y * g2) / det,
-                       (x23.z * g0 + x31.z * g1 + x12.z * g2) / det};
-  const double u = hu[i], v = hv[i];
-  const double b[3] = {1.0 - u - v, u, v};
+  // The 3x3 solve runs in float-float arithmetic (common.cuh): for grazing
+  // rays det M is small and a plain fp32 solve loses the digits the 1e-3
+  // gradient bar needs; the edges p0-p1, p0-p2 are formed exactly.
+  float pv[3][3];
+  for (int k = 0; k < 3; ++k)
+    for (int a = 0; a < 3; ++a) pv[k][a] = pos[3 * vi[k] + a];
+  const dfl c1[3] = {dfl{dx[i], 0.0f}, dfl{dy[i], 0.0f}, dfl{dz[i], 0.0f}};
+  dfl c2[3], c3[3];
+  for (int a = 0; a < 3; ++a) {
+    c2[a] = two_sum(pv[0][a], -pv[1][a]);
+    c3[a] = two_sum(pv[0][a], -pv[2][a]);
+  }
+  dfl x23[3], x31[3], x12[3];
+  crossdf(c2, c3, x23);
+  crossdf(c3, c1, x31);
+  crossdf(c1, c2, x12);
+  const dfl det = df_add(df_add(df_mul(c1[0], x23[0]), df_mul(c1[1], x23[1])), df_mul(c1[2], x23[2]));
+  if (det.hi == 0.0f) return;
+  float w[3];
+  for (int a = 0; a < 3; ++a) {
+    const dfl num = df_add(df_add(df_mulf(x23[a], g0), df_mulf(x31[a], g1)), df_mulf(x12[a], g2));
+    const dfl q = df_div(num, det);
+    w[a] = q.hi + q.lo;
+  }
+  const float u = hu[i], v = hv[i];
+  const float b[3] = {1.0f - u - v, u, v};
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    atomicAdd(grad + 3 * vi[k], (float)(b[k] * w[0]));
-    atomicAdd(grad + 3 * vi[k] + 1, (float)(b[k] * w[1]));
-    atomicAdd(grad + 3 * vi[k] + 2, (float)(b[k] * w[2]));
+    atomicAdd(grad + 3 * vi[k], b[k] * w[0]);
+    atomicAdd(grad + 3 * vi[k] + 1, b[k] * w[1]);
+    atomicAdd(grad + 3 * vi[k] + 2, b[k] * w[2]);
   }
 }
 

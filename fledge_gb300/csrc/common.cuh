@@ -207,34 +207,86 @@ __device__ __forceinline__ bool pluecker(float3 a, float3 b, float3 c, float3 O,
   return true;
 }
 
-// Hit values of the selected triangle recomputed in double precision (same
-// Pluecker quantities: t = (v0.N)/(N.D) with N = e0 x e1, u = U/S, v = V/S)
-// and rounded once to fp32.  The fp32 test above decides hit/miss and which
-// triangle is closest; this makes the reported t, u, v accurate to an ulp
-// even for grazing rays, where the fp32 quotient loses digits.  Leaves the
-// inputs unchanged when the double-precision plane is degenerate.
+// --------------------------------------------------------------------------
+// Float-float ("double-word") arithmetic on the FP32 pipe: a value is an
+// unevaluated sum hi + lo of two floats (error-free transforms of Knuth and
+// Dekker; multiplication with FMA, as analysed by Joldes, Muller and Popescu,
+// "Tight and rigorous error bounds for basic building blocks of double-word
+// arithmetic", 2017).  About 44 significant bits.  GB300's FP64 rate is far
+// too low for a per-ray step, so the refinement below uses this instead.
+// --------------------------------------------------------------------------
+struct dfl {
+  float hi, lo;
+};
+__device__ __forceinline__ dfl two_sum(float a, float b) {
+  float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ dfl fast_two_sum(float a, float b) {
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ dfl df_add(dfl x, dfl y) {
+  dfl s = two_sum(x.hi, y.hi), t = two_sum(x.lo, y.lo);
+  dfl v = fast_two_sum(s.hi, s.lo + t.hi);
+  return fast_two_sum(v.hi, t.lo + v.lo);
+}
+__device__ __forceinline__ dfl df_sub(dfl x, dfl y) { return df_add(x, dfl{-y.hi, -y.lo}); }
+__device__ __forceinline__ dfl df_mul(dfl x, dfl y) {
+  float p = x.hi * y.hi;
+  float e = fmaf(x.hi, y.hi, -p);
+  e = fmaf(x.hi, y.lo, e);
+  e = fmaf(x.lo, y.hi, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ dfl df_mulf(dfl x, float y) {
+  float p = x.hi * y;
+  float e = fmaf(x.hi, y, -p);
+  e = fmaf(x.lo, y, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ dfl df_div(dfl x, dfl y) {
+  float q1 = x.hi / y.hi;
+  dfl r = df_sub(x, df_mulf(y, q1));
+  float q2 = r.hi / y.hi;
+  return fast_two_sum(q1, q2);
+}
+
+// Hit values of the selected triangle recomputed in float-float with the
+// same Pluecker quantities (t = (v0.N)/(N.D), N = e0 x e1; u = U/S, v = V/S
+// with S = U+V+W = 2 N.D) and rounded once to fp32.  The fp32 test decides
+// hit/miss and which triangle is closest; this makes the reported t, u, v
+// accurate to about an ulp even for grazing rays, where the fp32 quotients
+// lose digits.  Edges are formed exactly (e0 = c - a, e1 = a - b as
+// float-float).  Leaves the inputs unchanged when N.D is zero.
 __device__ __forceinline__ void refine_tuv(float3 a, float3 b, float3 c, float3 O, float3 D, float &t, float &u,
                                            float &v) {
-  const double Ox = O.x, Oy = O.y, Oz = O.z, Dx = D.x, Dy = D.y, Dz = D.z;
-  const double v0x = (double)a.x - Ox, v0y = (double)a.y - Oy, v0z = (double)a.z - Oz;
-  const double v1x = (double)b.x - Ox, v1y = (double)b.y - Oy, v1z = (double)b.z - Oz;
-  const double v2x = (double)c.x - Ox, v2y = (double)c.y - Oy, v2z = (double)c.z - Oz;
-  const double e0x = v2x - v0x, e0y = v2y - v0y, e0z = v2z - v0z;
-  const double e1x = v0x - v1x, e1y = v0y - v1y, e1z = v0z - v1z;
-  const double e2x = v1x - v2x, e2y = v1y - v2y, e2z = v1z - v2z;
-  const double s0x = v2x + v0x, s0y = v2y + v0y, s0z = v2z + v0z;
-  const double s1x = v0x + v1x, s1y = v0y + v1y, s1z = v0z + v1z;
-  const double s2x = v1x + v2x, s2y = v1y + v2y, s2z = v1z + v2z;
-  const double U = (e0y * s0z - e0z * s0y) * Dx + (e0z * s0x - e0x * s0z) * Dy + (e0x * s0y - e0y * s0x) * Dz;
-  const double V = (e1y * s1z - e1z * s1y) * Dx + (e1z * s1x - e1x * s1z) * Dy + (e1x * s1y - e1y * s1x) * Dz;
-  const double W = (e2y * s2z - e2z * s2y) * Dx + (e2z * s2x - e2x * s2z) * Dy + (e2x * s2y - e2y * s2x) * Dz;
-  const double S = U + V + W;
-  const double Nx = e0y * e1z - e0z * e1y, Ny = e0z * e1x - e0x * e1z, Nz = e0x * e1y - e0y * e1x;
-  const double den = Nx * Dx + Ny * Dy + Nz * Dz;
-  if (den == 0.0 || S == 0.0) return;
-  t = (float)((v0x * Nx + v0y * Ny + v0z * Nz) / den);
-  u = (float)(U / S);
-  v = (float)(V / S);
+  const dfl e0x = two_sum(c.x, -a.x), e0y = two_sum(c.y, -a.y), e0z = two_sum(c.z, -a.z);
+  const dfl e1x = two_sum(a.x, -b.x), e1y = two_sum(a.y, -b.y), e1z = two_sum(a.z, -b.z);
+  const dfl v0x = two_sum(a.x, -O.x), v0y = two_sum(a.y, -O.y), v0z = two_sum(a.z, -O.z);
+  const dfl v1x = two_sum(b.x, -O.x), v1y = two_sum(b.y, -O.y), v1z = two_sum(b.z, -O.z);
+  const dfl v2x = two_sum(c.x, -O.x), v2y = two_sum(c.y, -O.y), v2z = two_sum(c.z, -O.z);
+  const dfl s0x = df_add(v2x, v0x), s0y = df_add(v2y, v0y), s0z = df_add(v2z, v0z);
+  const dfl s1x = df_add(v0x, v1x), s1y = df_add(v0y, v1y), s1z = df_add(v0z, v1z);
+  // U = (e0 x s0) . D, V = (e1 x s1) . D
+  const dfl U = df_add(df_add(df_mulf(df_sub(df_mul(e0y, s0z), df_mul(e0z, s0y)), D.x),
+                              df_mulf(df_sub(df_mul(e0z, s0x), df_mul(e0x, s0z)), D.y)),
+                       df_mulf(df_sub(df_mul(e0x, s0y), df_mul(e0y, s0x)), D.z));
+  const dfl V = df_add(df_add(df_mulf(df_sub(df_mul(e1y, s1z), df_mul(e1z, s1y)), D.x),
+                              df_mulf(df_sub(df_mul(e1z, s1x), df_mul(e1x, s1z)), D.y)),
+                       df_mulf(df_sub(df_mul(e1x, s1y), df_mul(e1y, s1x)), D.z));
+  // N = e0 x e1
+  const dfl Nx = df_sub(df_mul(e0y, e1z), df_mul(e0z, e1y));
+  const dfl Ny = df_sub(df_mul(e0z, e1x), df_mul(e0x, e1z));
+  const dfl Nz = df_sub(df_mul(e0x, e1y), df_mul(e0y, e1x));
+  const dfl den = df_add(df_add(df_mulf(Nx, D.x), df_mulf(Ny, D.y)), df_mulf(Nz, D.z));
+  if (den.hi == 0.0f) return;
+  const dfl num = df_add(df_add(df_mul(v0x, Nx), df_mul(v0y, Ny)), df_mul(v0z, Nz));
+  const dfl S = dfl{2.0f * den.hi, 2.0f * den.lo};
+  const dfl tt = df_div(num, den), uu = df_div(U, S), vv = df_div(V, S);
+  t = tt.hi + tt.lo;
+  u = uu.hi + uu.lo;
+  v = vv.hi + vv.lo;
 }
 
 // Accept a candidate t for closest hit: tmin <= t, and t < best (or t == best

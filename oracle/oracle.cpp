@@ -307,6 +307,80 @@ inline bool pluecker64(const float *fa, const float *fb, const float *fc, const 
   return true;
 }
 
+// Float-float arithmetic (error-free transforms: Knuth/Dekker two-sum, FMA
+// two-product; Joldes, Muller, Popescu 2017).  std::fmaf is correctly rounded,
+// as is the GPU's fmaf, so these routines give the same bits on both sides.
+struct Dfl { float hi, lo; };
+inline Dfl two_sum(float a, float b) {
+  float s = a + b, bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+inline Dfl fast_two_sum(float a, float b) {
+  float s = a + b;
+  return {s, b - (s - a)};
+}
+inline Dfl df_add(Dfl x, Dfl y) {
+  Dfl s = two_sum(x.hi, y.hi), t = two_sum(x.lo, y.lo);
+  Dfl v = fast_two_sum(s.hi, s.lo + t.hi);
+  return fast_two_sum(v.hi, t.lo + v.lo);
+}
+inline Dfl df_sub(Dfl x, Dfl y) { return df_add(x, Dfl{-y.hi, -y.lo}); }
+inline Dfl df_mul(Dfl x, Dfl y) {
+  float p = x.hi * y.hi;
+  float e = std::fmaf(x.hi, y.hi, -p);
+  e = std::fmaf(x.hi, y.lo, e);
+  e = std::fmaf(x.lo, y.hi, e);
+  return fast_two_sum(p, e);
+}
+inline Dfl df_mulf(Dfl x, float y) {
+  float p = x.hi * y;
+  float e = std::fmaf(x.hi, y, -p);
+  e = std::fmaf(x.lo, y, e);
+  return fast_two_sum(p, e);
+}
+inline Dfl df_div(Dfl x, Dfl y) {
+  float q1 = x.hi / y.hi;
+  Dfl r = df_sub(x, df_mulf(y, q1));
+  float q2 = r.hi / y.hi;
+  return fast_two_sum(q1, q2);
+}
+
+// Reported hit values of the GPU path: the selected triangle's Pluecker t,
+// u, v recomputed in float-float (t = (v0.N)/(N.D), N = e0 x e1, u = U/S,
+// v = V/S, S = 2 N.D) and rounded once.
+inline void refine_tuv(const float *a, const float *b, const float *c, const float *O, const float *D, float &t,
+                       float &u, float &v) {
+  Dfl e0[3], e1[3], v0[3], v1[3], v2[3], s0[3], s1[3];
+  for (int k = 0; k < 3; ++k) {
+    e0[k] = two_sum(c[k], -a[k]);
+    e1[k] = two_sum(a[k], -b[k]);
+    v0[k] = two_sum(a[k], -O[k]);
+    v1[k] = two_sum(b[k], -O[k]);
+    v2[k] = two_sum(c[k], -O[k]);
+  }
+  for (int k = 0; k < 3; ++k) {
+    s0[k] = df_add(v2[k], v0[k]);
+    s1[k] = df_add(v0[k], v1[k]);
+  }
+  auto crossdot = [&](const Dfl *e, const Dfl *s) {
+    return df_add(df_add(df_mulf(df_sub(df_mul(e[1], s[2]), df_mul(e[2], s[1])), D[0]),
+                         df_mulf(df_sub(df_mul(e[2], s[0]), df_mul(e[0], s[2])), D[1])),
+                  df_mulf(df_sub(df_mul(e[0], s[1]), df_mul(e[1], s[0])), D[2]));
+  };
+  Dfl U = crossdot(e0, s0), V = crossdot(e1, s1);
+  Dfl N[3] = {df_sub(df_mul(e0[1], e1[2]), df_mul(e0[2], e1[1])),
+              df_sub(df_mul(e0[2], e1[0]), df_mul(e0[0], e1[2])),
+              df_sub(df_mul(e0[0], e1[1]), df_mul(e0[1], e1[0]))};
+  Dfl den = df_add(df_add(df_mulf(N[0], D[0]), df_mulf(N[1], D[1])), df_mulf(N[2], D[2]));
+  if (den.hi == 0.0f) return;
+  Dfl num = df_add(df_add(df_mul(v0[0], N[0]), df_mul(v0[1], N[1])), df_mul(v0[2], N[2]));
+  Dfl S = {2.0f * den.hi, 2.0f * den.lo};
+  Dfl tt = df_div(num, den), uu = df_div(U, S), vv = df_div(V, S);
+  t = tt.hi + tt.lo;
+  u = uu.hi + uu.lo;
+  v = vv.hi + vv.lo;
+}
+
 // BoundIntersect (intersector.hpp:103-120): t0 starts at 0, t1 at FLT_MAX.
 inline bool bound_intersect(const float *lo, const float *hi, const float *o, const float *inv,
                             float *tnear) {
@@ -737,15 +811,9 @@ ORC_API void orc_trace_closest(const float *pos, const int32_t *idx, int64_t n_t
       recursive_intersect(T, M, 0, r, mode, b);
     }
     if (mode == MODE_DEV && b.prim >= 0) {
-      // The GPU reports the selected triangle's t, u, v recomputed in double
-      // precision and rounded once (refine_tuv); same expression here.
-      double O[3] = {r.o[0], r.o[1], r.o[2]}, D[3] = {r.d[0], r.d[1], r.d[2]};
-      double t64, u64, v64;
-      if (pluecker64(M.v(b.prim, 0), M.v(b.prim, 1), M.v(b.prim, 2), O, D, &t64, &u64, &v64)) {
-        b.tfar = (float)t64;
-        b.u = (float)u64;
-        b.v = (float)v64;
-      }
+      // The GPU reports the selected triangle's t, u, v recomputed in
+      // float-float arithmetic and rounded once; same operations here.
+      refine_tuv(M.v(b.prim, 0), M.v(b.prim, 1), M.v(b.prim, 2), r.o, r.d, b.tfar, b.u, b.v);
     }
     prim[i] = b.prim;
     t[i] = b.prim >= 0 ? b.tfar : r.tmax;
