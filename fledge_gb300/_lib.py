@@ -81,6 +81,7 @@ SIGNATURES = {
     "flg_trace_closest_batched": [P, P, C.POINTER(FlgRays), C.POINTER(I64), C.POINTER(FlgTraceOpts),
                                   C.POINTER(FlgHits)],
     "flg_trace_closest_host": [P, P, C.POINTER(FlgRays), I64, C.POINTER(FlgTraceOpts), C.POINTER(FlgHits)],
+    "flg_trace_closest_noalloc": [P, P, C.POINTER(FlgRays), I64, C.POINTER(FlgHits)],
     "flg_autotune_trace": [P, P, C.POINTER(FlgRays), I64, C.POINTER(FlgTraceOpts), C.POINTER(I32),
                            C.c_char_p, C.c_size_t],
     "flg_bvh_set_width": [P, P, I32, I32],

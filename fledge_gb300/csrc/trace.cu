@@ -19,6 +19,7 @@
 #include <chrono>
 #include <climits>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -738,4 +739,96 @@ done:
     json[json_len - 1] = '\0';
   }
   return flg_ctx_sync(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// Closest hit that allocates nothing.
+//
+// flg_trace_closest takes its traversal scratch (the list of rays whose short
+// stack overflowed, plus two counters) from the context and allocates it with
+// cudaMalloc on the context's first trace.  Some callers cannot allocate at
+// that moment: a renderer recording its frame loop into a CUDA graph (an
+// allocation inside a stream capture is refused), an application whose
+// device memory is handed out once, up front, by its own arena (as the
+// reference's Resource arena owns every allocation, src/resource.hpp:45-120),
+// or a latency-critical loop in which a cudaMalloc would synchronise the
+// device.  This entry point runs the same traversal kernels with the scratch
+// in a fixed file-scope device array instead.
+//
+// The array holds the overflow list for at most kNoAllocMaxRays rays (8 MB
+// plus 256 bytes of counters) and stays resident on every GPU that loads the
+// library until the process exits.  All calls share it: calls that overlap
+// on the GPU (concurrent streams or contexts) race on it and must not be
+// issued.  Its counters are cleared at the start of every call.
+// ---------------------------------------------------------------------------
+constexpr int64_t kNoAllocMaxRays = int64_t(1) << 20;
+// words: [0] overflow count (low 32 bits), [1] work counter, [2, 32) unused,
+// [32, 32 + kNoAllocMaxRays) overflow list of ray indices
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[32 + kNoAllocMaxRays];
+
+static std::mutex g_noalloc_mu;
+static unsigned long long *g_noalloc_ptr[64] = {};
+
+// Device address of the scratch array on ctx's device.  In host code the
+// array's name is only a host-side stand-in, so the address is looked up
+// once per device with that device current, and cached.
+static int noalloc_scratch(flg_ctx ctx, unsigned long long **out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (ctx->device < 0 || ctx->device >= 64) return set_error(ctx, FLG_ERR_UNSUPPORTED, "device index >= 64");
+  if (!g_noalloc_ptr[ctx->device]) {
+    int prev = 0;
+    FLG_CUDA(ctx, cudaGetDevice(&prev));
+    FLG_CUDA(ctx, cudaSetDevice(ctx->device));
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    cudaError_t e2 = cudaSetDevice(prev);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "cudaSetDevice");
+    g_noalloc_ptr[ctx->device] = (unsigned long long *)p;
+  }
+  *out = g_noalloc_ptr[ctx->device];
+  return FLG_OK;
+}
+
+FLG_API int flg_trace_closest_noalloc(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n, flg_hits *out) {
+  if (!ctx || !bvh || !out) return ctx ? set_error(ctx, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
+  int rc = check_rays(ctx, rays, n);
+  if (rc) return rc;
+  if (n > kNoAllocMaxRays)
+    return set_error(ctx, FLG_ERR_ARG, "flg_trace_closest_noalloc: n = %lld exceeds its maximum of %lld rays",
+                     (long long)n, (long long)kNoAllocMaxRays);
+  if (n > 0 && (!out->prim || !out->t || !out->u || !out->v))
+    return set_error(ctx, FLG_ERR_ARG, "hit output pointer is NULL");
+  if (bvh->n_scenes != 1) return set_error(ctx, FLG_ERR_ARG, "batched handle: use flg_trace_closest_batched");
+  unsigned long long *s = nullptr;
+  if ((rc = noalloc_scratch(ctx, &s))) return rc;
+  if (n == 0) return FLG_OK;
+  cudaStream_t st = ctx->stream;
+  // Clear the shared counters left by the previous call.
+  FLG_CUDA(ctx, cudaMemsetAsync(s, 0, 2 * sizeof(unsigned long long), st));
+  Scratch S{(int64_t *)(s + 32), (uint32_t *)s, kNoAllocMaxRays, s + 1, ctx->d_err};
+  RaySoA R{rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmin, rays->tmax,
+           rays->tmin_const, rays->tmax_const};
+  Out O{out->prim, out->t, out->u, out->v, nullptr};
+  const unsigned g = (unsigned)ceil_div(n, 256);
+  const unsigned rg = (unsigned)ctx->num_sms;
+  if (bvh->width == 2) {
+    k_trace_bvh2<false><<<g, 256, 0, st>>>(bvh->d_nodes2, bvh->d_tris, bvh->d_root, nullptr, 1, R, n, O, S);
+    FLG_LAUNCH_CHECK(ctx, "k_trace_bvh2");
+    k_trace_retry<2, false><<<rg, 128, 0, st>>>(nullptr, bvh->d_nodes2, bvh->d_tris, bvh->d_root, nullptr, 1, R, O, S);
+  } else if (bvh->width == 4) {
+    k_trace_wide<4, false, 64><<<g, 256, 0, st>>>((const NodeW<4> *)bvh->d_wide, bvh->d_tris, bvh->d_wide_root,
+                                                  nullptr, 1, R, n, O, S);
+    FLG_LAUNCH_CHECK(ctx, "k_trace_wide");
+    k_trace_retry<4, false><<<rg, 128, 0, st>>>((const NodeW<4> *)bvh->d_wide, bvh->d_nodes2, bvh->d_tris,
+                                                bvh->d_wide_root, nullptr, 1, R, O, S);
+  } else {
+    k_trace_wide<8, false, 64><<<g, 256, 0, st>>>((const NodeW<8> *)bvh->d_wide, bvh->d_tris, bvh->d_wide_root,
+                                                  nullptr, 1, R, n, O, S);
+    FLG_LAUNCH_CHECK(ctx, "k_trace_wide");
+    k_trace_retry<8, false><<<rg, 128, 0, st>>>((const NodeW<8> *)bvh->d_wide, bvh->d_nodes2, bvh->d_tris,
+                                                bvh->d_wide_root, nullptr, 1, R, O, S);
+  }
+  FLG_LAUNCH_CHECK(ctx, "k_trace_retry");
+  return FLG_OK;
 }

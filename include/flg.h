@@ -184,6 +184,20 @@ FLG_API int flg_trace_closest_batched(flg_ctx ctx, flg_bvh bvh, const flg_rays *
 FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays_host,
                                    int64_t n, const flg_trace_opts *opts, flg_hits *out_host);
 
+/* Closest hit that allocates nothing (no counterpart in the reference).  For
+ * callers that cannot call cudaMalloc when they trace — inside a CUDA stream
+ * capture, under an arena that hands out all device memory up front, or in a
+ * frame loop where an allocation would synchronise the device — whereas
+ * flg_trace_closest allocates its scratch on a context's first trace.  Same
+ * kernels and results as flg_trace_closest with default options; the
+ * scratch is a fixed 8 MB device array inside the library, held on every GPU
+ * that loads it until exit.  At most 1,048,576 rays per call (larger n:
+ * FLG_ERR_ARG).  The first call on a device looks the array up
+ * (cudaGetSymbolAddress) and should come before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race. */
+FLG_API int flg_trace_closest_noalloc(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n,
+                                      flg_hits *out);
+
 /* Sweeps node width (2/4/8), stack depth (32/64), persistent kernel on/off
  * with refill thresholds and ray sorting on the given workload, keeps the
  * fastest in *best and writes a JSON record (NUL-terminated) to json_out. */
