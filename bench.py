@@ -214,6 +214,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         ps = [C.c_void_p(soa[k, c0:].data_ptr()) for k in range(6)]
         cen = (C.c_float * 3)(0.5, 0.5, 0.5)
         ctx.check(lib.flg_gen_rays(ctx.h, SEED_C3 + 1, c0, m, cen, 2.0, *ps))
+    if args.presort_rays:
+        log("presorting rays (diagnostics)")
+        presort_rays(torch, soa, roffs)
     rays = F.Rays.from_soa(soa, tmin=1e-4)
     hits = {"prim": torch.empty(n_rays, dtype=torch.int32, device=dev),
             "t": torch.empty(n_rays, dtype=torch.float32, device=dev),
@@ -326,6 +329,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     # ---- volume: config 2 forward + adjoint ----
     log('e2e done')
     vol = run_volume(ctx, torch, F, dev) if not args.skip_volume else None
+    log("config 0")
+    c0 = run_c0(ctx, torch, F, dev, pk) if not args.skip_c0 else None
+    log("config 4")
+    c4 = run_c4(ctx, torch, F, dev, pk) if not args.skip_c4 else None
 
     # ---- CPU baseline (rank 0) ----
     log('volume done')
@@ -355,6 +362,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                            "parallelism": f"replicas x{world}"},
                 "build_ms": round(b_ms, 3), "trace_ms": round(tr_ms, 3), "hit_rate": round(hit_rate, 4),
                 "build_roofline": build_roof, "roofline": roof, "plain": plain, "volume": vol,
+                "config0": c0, "config4": c4,
                 "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches),
                 "gpu_launches_total": int(total_launches)}
         print(json.dumps(line), flush=True)
@@ -437,6 +445,131 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
             "ms_per_step": round(dt * 1e3, 3), "host_readback_consistent": ok}
 
 
+BYTES_PER_TRI_SINGLE = 36 + 44 + (4 + 4 * 16) + 20 + 100
+
+
+def presort_rays(torch, soa, roffs):
+    """Diagnostics: reorder every scene's rays by a 6-D Morton key of origin
+    and direction (4 bits per coordinate) to measure what ray coherence buys."""
+    def spread(x):  # 4 bits -> every 6th bit
+        out = torch.zeros_like(x)
+        for b in range(4):
+            out |= ((x >> b) & 1) << (6 * b)
+        return out
+    for s in range(len(roffs) - 1):
+        a, b = int(roffs[s]), int(roffs[s + 1])
+        if b - a < 2:
+            continue
+        seg = soa[:, a:b]
+        key = torch.zeros(b - a, dtype=torch.int64, device=soa.device)
+        for k in range(6):
+            lo, hi = (-1.6, 2.6) if k < 3 else (-1.0, 1.0)
+            q = ((seg[k] - lo) / (hi - lo) * 16).clamp(0, 15).to(torch.int64)
+            key |= spread(q) << k
+        order = torch.argsort(key)
+        soa[:, a:b] = seg[:, order]
+
+
+def _time(torch, fn, reps, stream):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fn()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_c0(ctx, torch, F, dev, pk):
+    """Config 0: 65,536 triangles, 1,048,576 rays: build ms and closest-hit
+    Mrays/s for the plain BVH2 kernel and the 4-wide kernel."""
+    s = torch.cuda.current_stream(dev)
+    pos = F.gen_triangles(ctx, 65536, SEED_C0)
+    rays = F.Rays.from_soa(F.gen_rays(ctx, 1 << 20, SEED_C0 + 1), tmin=1e-4)
+    out = {}
+    for w in (2, 4):
+        b = F.RadixBVHBuilder(F.InternalTriangleMesh(pos), ctx, node_width=w)
+        b.build()
+        hits = b.intersect(rays)
+        bms = _time(torch, b.build, 20, s)
+        tms = _time(torch, lambda: b.intersect(rays, out=hits), 20, s)
+        out[f"w{w}"] = {"build_ms": round(bms, 4), "trace_ms": round(tms, 4),
+                        "mrays_s": round((1 << 20) / (tms * 1e-3) / 1e6, 1)}
+        b.destroy()
+    out["build_roofline_frac"] = round(65536 * BYTES_PER_TRI_SINGLE / (out["w2"]["build_ms"] * 1e-3) / 1e9
+                                       / pk["hbm_gbs"], 4)
+    return out
+
+
+def run_c4(ctx, torch, F, dev, pk):
+    """Config 4: an 8 M-triangle random soup inside a 512^3 noise volume;
+    3840x2160x4 camera rays (closest hit), one shadow ray per hit toward a
+    point light (any hit), transmittance of the camera rays through the volume
+    with its adjoint (checkpointed), and the hit adjoint w.r.t. vertices."""
+    s = torch.cuda.current_stream(dev)
+    n_tri = 8_000_000
+    pos = F.gen_triangles(ctx, n_tri, SEED_C3 + 40)
+    b = F.RadixBVHBuilder(F.InternalTriangleMesh(pos), ctx, node_width=4)
+    b.build()
+    bms = _time(torch, b.build, 5, s)
+    W, H, spp = 3840, 2160, 4
+    n = W * H * spp
+    g = torch.Generator(device=dev).manual_seed(SEED_C3 + 41)
+    pix = torch.arange(n, device=dev)
+    px = (pix // spp) % W
+    py = (pix // spp) // W
+    jx = torch.rand(n, device=dev, generator=g)
+    jy = torch.rand(n, device=dev, generator=g)
+    tan = math.tan(math.radians(22.5))
+    sx = ((px.float() + jx) / W * 2 - 1) * tan * (W / H)
+    sy = (1 - (py.float() + jy) / H * 2) * tan
+    d = torch.stack([sx, sy, torch.ones_like(sx)], 0)
+    d = d / d.norm(dim=0, keepdim=True)
+    o = torch.tensor([0.5, 0.5, -1.5], device=dev)[:, None].expand(3, n)
+    soa = torch.cat([o, d], 0).contiguous()
+    rays = F.Rays.from_soa(soa, tmin=1e-4)
+    hits = b.intersect(rays)
+    tms = _time(torch, lambda: b.intersect(rays, out=hits), 3, s)
+    # shadow rays toward a point light
+    light = torch.tensor([0.5, 2.0, 0.5], device=dev)[:, None]
+    hp = o + d * hits["t"][None, :]
+    sd = light - hp
+    dist = sd.norm(dim=0)
+    sd = sd / dist
+    hit = hits["prim"] >= 0
+    n_sh = int(hit.sum())
+    sh = torch.cat([hp[:, hit], sd[:, hit], torch.full((1, n_sh), 1e-4, device=dev),
+                    (dist[hit] * (1 - 1e-4))[None, :]], 0).contiguous()
+    srays = F.Rays(*[sh[k] for k in range(8)])
+    occ = b.intersectP(srays)
+    sms = _time(torch, lambda: b.intersectP(srays, out=occ), 3, s)
+    # volume over the same box
+    rho = F.gen_noise_grid(ctx, 512, SEED_C2 + 40)
+    vol = F.DenseGridVolume(rho, medium=F.Medium(0.8, 0.2, 0.3, 0.1, 0.0), ctx=ctx)
+    T, ck = vol.tr(rays, 5, checkpoint=True)
+    grad = torch.zeros_like(rho)
+    dL = torch.ones_like(T)
+    fwd = _time(torch, lambda: vol.tr(rays, 5, checkpoint=True), 3, s)
+    adj = _time(torch, lambda: vol.tr_adjoint(rays, 5, dL, T, ck, grad), 3, s)
+    gpos = torch.zeros_like(pos)
+    ones = torch.ones(n, device=dev)
+    hadj = _time(torch, lambda: F.hit_adjoint(ctx, F.InternalTriangleMesh(pos), rays, hits, ones, None, None, gpos),
+                 3, s)
+    ctx.sync()
+    res = {"workload": "config 4: 8M triangles, 512^3 grid, 3840x2160x4 camera + shadow rays",
+           "build_ms": round(bms, 3),
+           "build_roofline_frac": round(n_tri * BYTES_PER_TRI_SINGLE / (bms * 1e-3) / 1e9 / pk["hbm_gbs"], 4),
+           "primary_mrays_s": round(n / (tms * 1e-3) / 1e6, 1), "hit_rate": round(float(hit.float().mean()), 4),
+           "shadow_mrays_s": round(n_sh / (sms * 1e-3) / 1e6, 1), "occluded": round(float(occ.float().mean()), 4),
+           "tr_fwd_ms": round(fwd, 3), "tr_adj_ms": round(adj, 3), "adj_over_fwd": round(adj / fwd, 3),
+           "hit_adjoint_ms": round(hadj, 3)}
+    vol.destroy()
+    b.destroy()
+    return res
+
+
 def run_volume(ctx, torch, F, dev):
     """Config 2: 256^3 value-noise grid in [0,4], 4,194,304 rays, ratio
     tracking forward (with checkpoints) and adjoint."""
@@ -486,10 +619,14 @@ def main() -> None:
     ap.add_argument("--refill", type=int, default=16)
     ap.add_argument("--persistent", type=int, default=1)
     ap.add_argument("--stack", type=int, default=64)
+    ap.add_argument("--presort-rays", action="store_true",
+                    help="diagnostics only: reorder each scene's rays by a 6-D Morton key before timing")
     ap.add_argument("--plain-steps", type=int, default=1)
     ap.add_argument("--skip-plain", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-volume", action="store_true")
+    ap.add_argument("--skip-c0", action="store_true")
+    ap.add_argument("--skip-c4", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--scenes", type=int, default=256, help="diagnostics only: first N scenes")
     ap.add_argument("--verbose", action="store_true", help="progress on stderr")

@@ -15,6 +15,8 @@
 //                      arrival counters (radix_bvh.cpp:163-199); each child
 //                      box is written once, into its parent's record
 //   6. (optional) collapse to 4- or 8-wide nodes (collapse.cu)
+#include <cuda/atomic>
+
 #include <algorithm>
 #include <climits>
 #include <cstring>
@@ -234,25 +236,21 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// Child box of side s lives in float4 s (x/y lo-hi) and float2 s of the third
+// float4 (z lo-hi): one 16-byte and one 8-byte access each way.
 __device__ __forceinline__ void store_child_box(Node2 *nd, int side, const float *lo, const float *hi) {
-  float *f = (float *)nd;
-  if (side == 0) {
-    __stcg(f + 0, lo[0]); __stcg(f + 1, hi[0]); __stcg(f + 2, lo[1]); __stcg(f + 3, hi[1]);
-    __stcg(f + 8, lo[2]); __stcg(f + 9, hi[2]);
-  } else {
-    __stcg(f + 4, lo[0]); __stcg(f + 5, hi[0]); __stcg(f + 6, lo[1]); __stcg(f + 7, hi[1]);
-    __stcg(f + 10, lo[2]); __stcg(f + 11, hi[2]);
-  }
+  float4 *f4 = (float4 *)nd;
+  float2 *f2 = (float2 *)(f4 + 2);
+  __stcg(f4 + side, make_float4(lo[0], hi[0], lo[1], hi[1]));
+  __stcg(f2 + side, make_float2(lo[2], hi[2]));
 }
 __device__ __forceinline__ void load_child_box(const Node2 *nd, int side, float *lo, float *hi) {
-  const float *f = (const float *)nd;
-  if (side == 0) {
-    lo[0] = __ldcg(f + 0); hi[0] = __ldcg(f + 1); lo[1] = __ldcg(f + 2); hi[1] = __ldcg(f + 3);
-    lo[2] = __ldcg(f + 8); hi[2] = __ldcg(f + 9);
-  } else {
-    lo[0] = __ldcg(f + 4); hi[0] = __ldcg(f + 5); lo[1] = __ldcg(f + 6); hi[1] = __ldcg(f + 7);
-    lo[2] = __ldcg(f + 10); hi[2] = __ldcg(f + 11);
-  }
+  const float4 *f4 = (const float4 *)nd;
+  const float2 *f2 = (const float2 *)(f4 + 2);
+  const float4 a = __ldcg(f4 + side);
+  const float2 z = __ldcg(f2 + side);
+  lo[0] = a.x; hi[0] = a.y; lo[1] = a.z; hi[1] = a.w;
+  lo[2] = z.x; hi[2] = z.y;
 }
 
 // One thread per sorted leaf: gather the triangle, then climb.  The first
@@ -297,10 +295,11 @@ __global__ void __launch_bounds__(256)
       }
       Node2 *nd = nodes + noff + cur;
       store_child_box(nd, side, lo, hi);
-      __threadfence();
-      uint32_t old = atomicAdd(&flags[noff + cur], 1u);
+      // Release: the box above is visible before the count; acquire: the
+      // sibling's box, published before its increment, is read after ours.
+      cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrival(flags[noff + cur]);
+      const uint32_t old = arrival.fetch_add(1u, cuda::memory_order_acq_rel);
       if (old == 0u) break;
-      __threadfence();
       float olo[3], ohi[3];
       load_child_box(nd, side ^ 1, olo, ohi);
       for (int k = 0; k < 3; ++k) {

@@ -23,17 +23,25 @@ struct alignas(16) Node2 {
   int4 d;    // child0, child1, parent (global, -1 root), scene
 };
 
-// Wide node of width W, structure of arrays inside the record.  Child refs:
-// >= 0 wide node index; < 0 leaf range ~(first << 3 | (count - 1)) over
-// sorted triangles; kEmptyChild = unused slot.
+// Wide node of width W with quantised child boxes (after Ylitie, Karras and
+// Laine, "Efficient incoherent ray traversal on GPUs through compressed wide
+// BVHs", HPG 2017): the node's lower corner `org`, a power-of-two scale per
+// axis (biased exponent in `ex`), and per child and axis an 8-bit lower and
+// upper plane, rounded outward so every child box contains its exact box.
+// Rows q[0..5] are lo.x, hi.x, lo.y, hi.y, lo.z, hi.z, one byte per child.
+// Child refs: >= 0 wide node index; < 0 leaf range ~(first << 3 | (count-1))
+// over sorted triangles; kEmptyChild = unused slot (its box is inverted).
+// 64 bytes for W = 4, 96 bytes for W = 8 (4 / 6 16-byte loads per visit).
 constexpr int32_t kEmptyChild = 0x7FFFFFFF;
 template <int W>
-struct alignas(16) NodeW {
-  float lox[W], hix[W], loy[W], hiy[W], loz[W], hiz[W];
+struct alignas(W == 4 ? 64 : 32) NodeW {
+  float org[3];
+  uint8_t ex[4];
+  uint8_t q[6][W];
   int32_t child[W];
 };
-static_assert(sizeof(NodeW<4>) == 112, "NodeW<4> layout");
-static_assert(sizeof(NodeW<8>) == 224, "NodeW<8> layout");
+static_assert(sizeof(NodeW<4>) == 64, "NodeW<4> layout");
+static_assert(sizeof(NodeW<8>) == 96, "NodeW<8> layout");
 
 // Sorted triangle record: v0.xyz + original (scene-local) id, v1, v2.
 struct alignas(16) TriRec {

@@ -238,6 +238,53 @@ __device__ __forceinline__ void sort_keys(uint64_t (&k)[W]) {
   }
 }
 
+// Tests the W children of a quantised wide node (4 or 6 16-byte loads).  Per
+// axis a child plane is t = q * (s / d) + (org - o) / d with one FMA; the near
+// and far values come from min/max (a NaN slab, 0 * inf, constrains nothing),
+// and the interval is widened by 2^-20 relative so that rounding never
+// rejects a box that contains a hit.  Returns the number of children hit with
+// tnear <= lim; their keys (tnear | ref) are in key[], misses are ~0.
+template <int W>
+__device__ __forceinline__ int visit_node(const NodeW<W> *__restrict__ node, const float3 &o, const float3 &inv,
+                                          float lim, uint64_t (&key)[W]) {
+  constexpr int NV = (int)sizeof(NodeW<W>) / 16;
+  constexpr int RW = W / 4;  // 32-bit words per quantised row
+  uint32_t u[4 * NV];
+  const uint4 *np = (const uint4 *)node;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    const uint4 q = __ldg(np + k);
+    u[4 * k] = q.x; u[4 * k + 1] = q.y; u[4 * k + 2] = q.z; u[4 * k + 3] = q.w;
+  }
+  const float sx = __uint_as_float((u[3] & 0xFFu) << 23) * inv.x;
+  const float sy = __uint_as_float(((u[3] >> 8) & 0xFFu) << 23) * inv.y;
+  const float sz = __uint_as_float(((u[3] >> 16) & 0xFFu) << 23) * inv.z;
+  const float bx = (__uint_as_float(u[0]) - o.x) * inv.x;
+  const float by = (__uint_as_float(u[1]) - o.y) * inv.y;
+  const float bz = (__uint_as_float(u[2]) - o.z) * inv.z;
+  int nh = 0;
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    const int32_t ref = (int32_t)u[4 + 6 * RW + k];
+    const int sh = 8 * (k & 3);
+    const float qlx = (float)((u[4 + 0 * RW + k / 4] >> sh) & 0xFFu);
+    const float qhx = (float)((u[4 + 1 * RW + k / 4] >> sh) & 0xFFu);
+    const float qly = (float)((u[4 + 2 * RW + k / 4] >> sh) & 0xFFu);
+    const float qhy = (float)((u[4 + 3 * RW + k / 4] >> sh) & 0xFFu);
+    const float qlz = (float)((u[4 + 4 * RW + k / 4] >> sh) & 0xFFu);
+    const float qhz = (float)((u[4 + 5 * RW + k / 4] >> sh) & 0xFFu);
+    const float x0 = fmaf(qlx, sx, bx), x1 = fmaf(qhx, sx, bx);
+    const float y0 = fmaf(qly, sy, by), y1 = fmaf(qhy, sy, by);
+    const float z0 = fmaf(qlz, sz, bz), z1 = fmaf(qhz, sz, bz);
+    const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
+    const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), lim));
+    const bool ok = ref != kEmptyChild && tn * 0.99999905f <= tf * 1.00000095f;
+    key[k] = ok ? stack_key(tn, ref) : ~0ull;
+    nh += ok ? 1 : 0;
+  }
+  return nh;
+}
+
 template <int W, bool ANY, int STACK>
 struct Tracer {
   float3 o, d, inv;
@@ -272,25 +319,8 @@ struct Tracer {
   __device__ __forceinline__ bool step(const NodeW<W> *__restrict__ nodes, const TriRec *__restrict__ tris) {
     if (cur == kEmptyChild || cur == INT32_MIN) return true;
     if (cur >= 0) {
-      constexpr int NV = 7 * W / 4;  // float4 per record
-      float f[4 * NV];
-      const float4 *np = (const float4 *)(nodes + cur);
-#pragma unroll
-      for (int k = 0; k < NV; ++k) {
-        float4 q = __ldg(np + k);
-        f[4 * k] = q.x; f[4 * k + 1] = q.y; f[4 * k + 2] = q.z; f[4 * k + 3] = q.w;
-      }
-      const float lim = ANY ? tmax : best;
       uint64_t key[W];
-      int nh = 0;
-#pragma unroll
-      for (int k = 0; k < W; ++k) {
-        const int32_t ref = __float_as_int(f[6 * W + k]);
-        float t = slab_tnear(f[k], f[W + k], f[2 * W + k], f[3 * W + k], f[4 * W + k], f[5 * W + k], o, inv);
-        const bool ok = ref != kEmptyChild && t <= lim;
-        key[k] = ok ? stack_key(t, ref) : ~0ull;
-        nh += ok ? 1 : 0;
-      }
+      const int nh = visit_node<W>(nodes + cur, o, inv, ANY ? tmax : best, key);
       if (nh == 0) return !pop();
       sort_keys<W>(key);
       if (sp + nh - 1 > STACK) {
@@ -437,12 +467,154 @@ static int check_rays(flg_ctx ctx, const flg_rays *r, int64_t n) {
   return FLG_OK;
 }
 
+// ----------------------------------------------------------------------------
+// Persistent while-while traversal with speculative leaf postponing (Aila &
+// Laine, "Understanding the efficiency of ray traversal on GPUs", HPG 2009),
+// on wide nodes.  Each lane walks inner nodes; a lane that reaches a leaf
+// parks it and keeps walking inner nodes until every lane of the warp holds a
+// parked leaf (or has no inner node left); then the warp tests leaves
+// together.  Node and leaf code thus run with most lanes active, instead of
+// the two branches diverging at every step.  Finished lanes are refilled from
+// the global ray counter once `refill` of them are idle.
+// ----------------------------------------------------------------------------
+template <int W, bool ANY, int STACK>
+__global__ void __launch_bounds__(256, 4)
+    k_trace_ww(const NodeW<W> *__restrict__ nodes, const TriRec *__restrict__ tris, const int32_t *__restrict__ roots,
+               const int64_t *__restrict__ ray_off, int n_scenes, RaySoA R, int64_t n, Out O, Scratch S, int refill) {
+  constexpr int32_t kNone = kEmptyChild;  // "no node" / "no parked leaf"
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt = (1u << lane) - 1u;
+  float3 o = make_float3(0.f, 0.f, 0.f), d = o, inv = o;
+  float tmin = 0.f, tmax = 0.f, best = 0.f, hu = 0.f, hv = 0.f;
+  int32_t prim = -1, cur = kNone, leaf = kNone;
+  int sp = 0;
+  bool have = false, active = false, overflow = false, exhausted = false;
+  int64_t ray = -1;
+  uint64_t stk[STACK];
+
+  auto pop = [&]() -> int32_t {
+    const float lim = ANY ? tmax : best;
+    while (sp > 0) {
+      const uint64_t e = stk[--sp];
+      if (__uint_as_float((uint32_t)(e >> 32)) > lim) continue;
+      return (int32_t)(uint32_t)e;
+    }
+    return kNone;
+  };
+
+  while (true) {
+    // Retire finished rays.
+    if (active && cur == kNone && leaf == kNone) {
+      if (overflow) record_overflow(S, ray);
+      else write_result(O, ray, ANY, have, prim, best, tmax, hu, hv, tris, o, d);
+      active = false;
+    }
+    // Refill idle lanes.
+    const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active);
+    const int nidle = __popc(idle);
+    if (!exhausted && nidle >= refill) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(S.work, (unsigned long long)nidle);
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (!active) {
+        const int64_t my = (int64_t)base + __popc(idle & lt);
+        if (my < n) {
+          ray = my;
+          load_ray(R, ray, o, d, inv, tmin, tmax);
+          best = tmax;
+          have = false;
+          overflow = false;
+          prim = -1;
+          hu = hv = 0.0f;
+          sp = 0;
+          leaf = kNone;
+          cur = scene_root(roots, ray_off, n_scenes, ray);
+          if (cur == INT32_MIN) cur = kNone;
+          active = true;
+        }
+      }
+      if ((int64_t)base + nidle >= n) exhausted = true;
+    }
+    if (__ballot_sync(0xFFFFFFFFu, active) == 0u) {
+      if (exhausted) break;
+      continue;
+    }
+
+    // Inner nodes, parking the first leaf found.
+    while (true) {
+      if (active && cur < 0 && leaf == kNone) {
+        leaf = cur;
+        cur = pop();
+      }
+      const bool at_node = active && cur >= 0 && cur != kNone;
+      if (!__any_sync(0xFFFFFFFFu, at_node)) break;
+      if (at_node) {
+        uint64_t key[W];
+        const int nh = visit_node<W>(nodes + cur, o, inv, ANY ? tmax : best, key);
+        if (nh == 0) {
+          cur = pop();
+        } else {
+          sort_keys<W>(key);
+          if (sp + nh - 1 > STACK) {
+            overflow = true;
+            cur = kNone;
+            leaf = kNone;
+          } else {
+#pragma unroll
+            for (int k = W - 1; k >= 1; --k)
+              if (k < nh) stk[sp++] = key[k];
+            cur = (int32_t)(uint32_t)key[0];
+          }
+        }
+      }
+      // Leave once every active lane has parked a leaf or run out of nodes.
+      const bool ready = !active || leaf != kNone || cur == kNone || (cur < 0 && leaf != kNone);
+      if (__all_sync(0xFFFFFFFFu, ready)) break;
+    }
+
+    // Test the parked leaves together.
+    if (active && leaf != kNone) {
+      const int32_t enc = ~leaf;
+      const int64_t first = (int64_t)((uint32_t)enc >> 3);
+      const int count = (enc & 7) + 1;
+      for (int j = 0; j < count; ++j) {
+        if (ANY) {
+          if (test_tri_any(tris, first + j, o, d, tmin, tmax)) {
+            have = true;
+            cur = kNone;
+            break;
+          }
+        } else {
+          test_tri(tris, first + j, o, d, tmin, best, have, prim, hu, hv);
+        }
+      }
+      leaf = kNone;
+    }
+  }
+}
+
 template <int W, bool ANY>
 static void launch_wide(flg_ctx ctx, cudaStream_t st, flg_bvh b, const RaySoA &R, int64_t n, const Out &O,
                         const Scratch &S, const int64_t *ray_off, int n_scenes, const flg_trace_opts &op) {
   const NodeW<W> *nodes = (const NodeW<W> *)b->d_wide;
   const int threads = op.block_threads;
-  if (op.persistent) {
+  if (op.persistent == 2) {
+    int per_sm = 0;
+    if (op.stack_depth <= 32)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_ww<W, ANY, 32>, threads, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_ww<W, ANY, 64>, threads, 0);
+    if (per_sm < 1) per_sm = 1;
+    int64_t g = std::min<int64_t>((int64_t)per_sm * ctx->num_sms, ceil_div(n, threads));
+    if (g < 1) g = 1;
+    const int refill = std::max(1, std::min(32, op.refill_lanes));
+    if (op.stack_depth <= 32)
+      k_trace_ww<W, ANY, 32><<<(unsigned)g, threads, 0, st>>>(nodes, b->d_tris, b->d_wide_root, ray_off, n_scenes, R,
+                                                              n, O, S, refill);
+    else
+      k_trace_ww<W, ANY, 64><<<(unsigned)g, threads, 0, st>>>(nodes, b->d_tris, b->d_wide_root, ray_off, n_scenes, R,
+                                                              n, O, S, refill);
+  } else if (op.persistent) {
     int per_sm = 0;
     if (op.stack_depth <= 32)
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_persistent<W, ANY, 32>, threads, 0);
@@ -672,7 +844,7 @@ FLG_API int flg_autotune_trace(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, i
       if (rc) goto done;
       for (int stack : {32, 64}) {
         if (w == 2 && stack == 32) continue;
-        for (int pers : {0, 1}) {
+        for (int pers : {0, 1, 2}) {
           if (w == 2 && pers) continue;
           static const int kRefill[3] = {8, 16, 24};
           for (int ri = 0; ri < (pers ? 3 : 1); ++ri) {

@@ -80,7 +80,9 @@ typedef struct flg_build_opts {
 typedef struct flg_trace_opts {
   int32_t stack_depth;    /* 32 or 64 (0 = 64); overflowing rays are retried deeper */
   int32_t block_threads;  /* threads per block (0 = 256) */
-  int32_t persistent;     /* 1: persistent work-stealing kernel, 0: one ray per thread */
+  int32_t persistent;     /* 0: one ray per thread; 1: persistent work-stealing kernel;
+                             2: persistent while-while kernel with speculative leaf
+                             postponing (wide layouts) */
   int32_t refill_lanes;   /* persistent: refill a warp once this many lanes idle (0 = 16) */
   int32_t ray_sort;       /* 0: none; 1: sort rays by direction octant and origin cell */
 } flg_trace_opts;

@@ -23,7 +23,8 @@ def _batch(ctx, counts, rays_per_tri=8, seed=3, width=4):
     return bb, pos, soa, offs, roffs
 
 
-@pytest.mark.parametrize("opts", [{}, {"persistent": 1, "refill_lanes": 16}, {"persistent": 1, "refill_lanes": 1}])
+@pytest.mark.parametrize("opts", [{}, {"persistent": 1, "refill_lanes": 16}, {"persistent": 1, "refill_lanes": 1},
+                                  {"persistent": 2, "refill_lanes": 16}])
 def test_batched_trace_equals_per_scene(ctx, oracle, opts):
     import fledge_gb300 as F
     counts = [1, 2, 1000, 37, 20000, 5, 3000]

@@ -20,7 +20,9 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
 
 LAYOUTS = [(2, 1, {}), (4, 1, {}), (4, 4, {}), (8, 1, {}), (8, 2, {"stack_depth": 32}),
-           (4, 1, {"persistent": 1, "refill_lanes": 16}), (8, 4, {"persistent": 1, "refill_lanes": 8})]
+           (4, 1, {"persistent": 1, "refill_lanes": 16}), (8, 4, {"persistent": 1, "refill_lanes": 8}),
+           (4, 1, {"persistent": 2, "refill_lanes": 16}), (8, 2, {"persistent": 2, "refill_lanes": 1}),
+           (4, 4, {"persistent": 2, "refill_lanes": 32, "stack_depth": 32})]
 
 
 def _ids(v):
