@@ -278,8 +278,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     tr_ms = statistics.median(trace_ms)
     roof = {"bound": "hbm", "achieved": round(trace_bytes / (tr_ms * 1e-3) / 1e9, 1), "peak": pk["hbm_gbs"],
             "unit": "GB/s", "frac": None, "traffic": None,
-            "kernel": (f"k_trace_persistent<{width},false,{args.stack}>" if args.persistent and width > 2
-                       else f"k_trace_wide<{width},false,{args.stack}>" if width > 2 else "k_trace_bvh2<false>"),
+            "kernel": ("k_trace_bvh2<false>" if width == 2 else
+                       f"k_trace_ww<{width},false,{args.stack}>" if args.persistent == 2 else
+                       f"k_trace_persistent<{width},false,{args.stack}>" if args.persistent else
+                       f"k_trace_wide<{width},false,{args.stack}>"),
             "peak_source": pk["source"]}
     roof["frac"] = round(roof["achieved"] / roof["peak"], 4)
     b_ms = statistics.median(build_ms)
@@ -615,9 +617,11 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--width", type=int, default=4)
-    ap.add_argument("--leaf", type=int, default=1)
-    ap.add_argument("--refill", type=int, default=16)
-    ap.add_argument("--persistent", type=int, default=1)
+    # defaults: the fastest setting of the sweep over node width, leaf size,
+    # kernel kind and refill threshold on the first 32 scenes
+    ap.add_argument("--leaf", type=int, default=2)
+    ap.add_argument("--refill", type=int, default=8)
+    ap.add_argument("--persistent", type=int, default=2)
     ap.add_argument("--stack", type=int, default=64)
     ap.add_argument("--presort-rays", action="store_true",
                     help="diagnostics only: reorder each scene's rays by a 6-D Morton key before timing")

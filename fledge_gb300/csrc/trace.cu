@@ -262,22 +262,32 @@ __device__ __forceinline__ int visit_node(const NodeW<W> *__restrict__ node, con
   const float bx = (__uint_as_float(u[0]) - o.x) * inv.x;
   const float by = (__uint_as_float(u[1]) - o.y) * inv.y;
   const float bz = (__uint_as_float(u[2]) - o.z) * inv.z;
+  // Near and far plane rows per axis from the ray's direction signs (one
+  // select per packed word instead of a min/max per child and axis).
+  uint32_t nw[3][RW], fw[3][RW];
+  const bool neg[3] = {inv.x < 0.0f, inv.y < 0.0f, inv.z < 0.0f};
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int r = 0; r < RW; ++r) {
+      const uint32_t lo = u[4 + (2 * a) * RW + r], hi = u[4 + (2 * a + 1) * RW + r];
+      nw[a][r] = neg[a] ? hi : lo;
+      fw[a][r] = neg[a] ? lo : hi;
+    }
   int nh = 0;
 #pragma unroll
   for (int k = 0; k < W; ++k) {
     const int32_t ref = (int32_t)u[4 + 6 * RW + k];
-    const int sh = 8 * (k & 3);
-    const float qlx = (float)((u[4 + 0 * RW + k / 4] >> sh) & 0xFFu);
-    const float qhx = (float)((u[4 + 1 * RW + k / 4] >> sh) & 0xFFu);
-    const float qly = (float)((u[4 + 2 * RW + k / 4] >> sh) & 0xFFu);
-    const float qhy = (float)((u[4 + 3 * RW + k / 4] >> sh) & 0xFFu);
-    const float qlz = (float)((u[4 + 4 * RW + k / 4] >> sh) & 0xFFu);
-    const float qhz = (float)((u[4 + 5 * RW + k / 4] >> sh) & 0xFFu);
-    const float x0 = fmaf(qlx, sx, bx), x1 = fmaf(qhx, sx, bx);
-    const float y0 = fmaf(qly, sy, by), y1 = fmaf(qhy, sy, by);
-    const float z0 = fmaf(qlz, sz, bz), z1 = fmaf(qhz, sz, bz);
-    const float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
-    const float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), lim));
+    // byte k of a row word -> float: 0x4B0000qq is 2^23 + q exactly
+    const uint32_t sel = 0x7540u | (uint32_t)(k & 3);
+    const float qnx = __uint_as_float(__byte_perm(nw[0][k / 4], 0x4B000000u, sel)) - 8388608.0f;
+    const float qfx = __uint_as_float(__byte_perm(fw[0][k / 4], 0x4B000000u, sel)) - 8388608.0f;
+    const float qny = __uint_as_float(__byte_perm(nw[1][k / 4], 0x4B000000u, sel)) - 8388608.0f;
+    const float qfy = __uint_as_float(__byte_perm(fw[1][k / 4], 0x4B000000u, sel)) - 8388608.0f;
+    const float qnz = __uint_as_float(__byte_perm(nw[2][k / 4], 0x4B000000u, sel)) - 8388608.0f;
+    const float qfz = __uint_as_float(__byte_perm(fw[2][k / 4], 0x4B000000u, sel)) - 8388608.0f;
+    const float tn = fmaxf(fmaxf(fmaf(qnx, sx, bx), fmaf(qny, sy, by)), fmaxf(fmaf(qnz, sz, bz), 0.0f));
+    const float tf = fminf(fminf(fmaf(qfx, sx, bx), fmaf(qfy, sy, by)), fminf(fmaf(qfz, sz, bz), lim));
     const bool ok = ref != kEmptyChild && tn * 0.99999905f <= tf * 1.00000095f;
     key[k] = ok ? stack_key(tn, ref) : ~0ull;
     nh += ok ? 1 : 0;
