@@ -335,6 +335,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     c0 = run_c0(ctx, torch, F, dev, pk) if not args.skip_c0 else None
     log("config 4")
     c4 = run_c4(ctx, torch, F, dev, pk) if not args.skip_c4 else None
+    log("config 1")
+    c1 = run_c1(ctx, torch, F, dev, rank == 0 and not args.skip_cpu) if not args.skip_c1 else None
 
     # ---- CPU baseline (rank 0) ----
     log('volume done')
@@ -364,7 +366,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                            "parallelism": f"replicas x{world}"},
                 "build_ms": round(b_ms, 3), "trace_ms": round(tr_ms, 3), "hit_rate": round(hit_rate, 4),
                 "build_roofline": build_roof, "roofline": roof, "plain": plain, "volume": vol,
-                "config0": c0, "config4": c4,
+                "config0": c0, "config1": c1, "config4": c4,
                 "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches),
                 "gpu_launches_total": int(total_launches)}
         print(json.dumps(line), flush=True)
@@ -505,6 +507,50 @@ def run_c0(ctx, torch, F, dev, pk):
     return out
 
 
+C1_CAMERA = dict(eye=(0.0, 0.6, 3.5), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), fov_deg=40.0)
+
+
+def c1_scene():
+    from fledge_gb300.scenes import icosphere, quad_light
+    v, f = icosphere(8)
+    lv, lf = quad_light()
+    return np.concatenate([v, lv], 0), np.concatenate([f, lf + len(v)], 0), len(f)
+
+
+def run_c1(ctx, torch, F, dev, with_cpu: bool):
+    """Config 1: wavefront path tracing of the level-8 displaced icosphere
+    (1,310,720 triangles) under a 0.2 x 0.2 light, 1920x1080 at 16 spp,
+    depth 5: Mrays/s over all closest-hit and shadow rays."""
+    pos, ind, lfirst = c1_scene()
+    p, i = torch.from_numpy(pos).to(dev), torch.from_numpy(ind).to(dev)
+    b = F.RadixBVHBuilder(F.InternalTriangleMesh(p, i), ctx, node_width=4, leaf_size=2)
+    b.build()
+    F.pathtrace(ctx, b, lfirst, 2, width=1920, height=1080, spp=1, max_depth=5, **C1_CAMERA)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    img, stats = F.pathtrace(ctx, b, lfirst, 2, width=1920, height=1080, spp=16, max_depth=5, **C1_CAMERA)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    n = stats["closest_rays"] + stats["shadow_rays"]
+    res = {"workload": "config 1: 1,310,720-triangle displaced icosphere, 1920x1080x16 spp, depth 5",
+           "ms": round(dt * 1e3, 2), "mrays_s": round(n / dt / 1e6, 1), "closest_rays": stats["closest_rays"],
+           "shadow_rays": stats["shadow_rays"], "mean_radiance": round(float(img.mean()), 6)}
+    if with_cpu:
+        from oracle import oracle as O
+        O.build()
+        O.set_threads(os.cpu_count() or 1)
+        tree = O.build_bvh(pos, ind)
+        stride = 5
+        t0 = time.perf_counter()
+        _, rays = O.pathtrace(pos, ind, tree, lfirst, 2, (10, 10, 10), (0.7, 0.7, 0.7), C1_CAMERA["eye"],
+                              C1_CAMERA["target"], C1_CAMERA["up"], C1_CAMERA["fov_deg"], 1920, 1080, 16, 5, stride)
+        cdt = time.perf_counter() - t0
+        res["cpu_mrays_s"] = round(sum(rays) / cdt / 1e6, 3)
+        res["cpu_sample"] = f"every {stride}th pixel ({sum(rays)} rays, {cdt:.1f} s, {os.cpu_count()} threads)"
+    b.destroy()
+    return res
+
+
 def run_c4(ctx, torch, F, dev, pk):
     """Config 4: an 8 M-triangle random soup inside a 512^3 noise volume;
     3840x2160x4 camera rays (closest hit), one shadow ray per hit toward a
@@ -631,6 +677,7 @@ def main() -> None:
     ap.add_argument("--skip-volume", action="store_true")
     ap.add_argument("--skip-c0", action="store_true")
     ap.add_argument("--skip-c4", action="store_true")
+    ap.add_argument("--skip-c1", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--scenes", type=int, default=256, help="diagnostics only: first N scenes")
     ap.add_argument("--verbose", action="store_true", help="progress on stderr")

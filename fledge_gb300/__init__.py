@@ -361,6 +361,26 @@ def hit_adjoint(ctx: Context, mesh: InternalTriangleMesh, rays: Rays, hits, dLdt
     return grad
 
 
+def pathtrace(ctx: Context, bvh: RadixBVHBuilder, light_first: int, light_count: int, light_le=(10.0, 10.0, 10.0),
+              albedo=(0.7, 0.7, 0.7), eye=(0.0, 0.5, 4.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0),
+              fov_deg: float = 40.0, width: int = 1920, height: int = 1080, spp: int = 16, max_depth: int = 5,
+              **opts):
+    """Wavefront path tracing of the mesh of `bvh` (PathIntegrator::Li with
+    next-event estimation).  Returns (radiance [height, width, 3], stats)."""
+    torch = _torch()
+    mesh = bvh.mesh
+    sc = _lib.FlgPtScene(_ptr(mesh.p), _ptr(mesh.ind), mesh.n_tri, mesh.n_vert, light_first, light_count,
+                         (C.c_float * 3)(*light_le), (C.c_float * 3)(*albedo))
+    cam = _lib.FlgPtCamera((C.c_float * 3)(*eye), (C.c_float * 3)(*target), (C.c_float * 3)(*up), fov_deg,
+                           width, height)
+    out = torch.empty((height, width, 3), dtype=torch.float32, device=mesh.p.device)
+    st = _lib.FlgPtStats()
+    op = _trace_opts(**opts)
+    ctx.check(ctx.lib.flg_pathtrace(ctx.h, bvh.h, C.byref(sc), C.byref(cam), spp, max_depth, C.byref(op),
+                                    C.c_void_p(_ptr(out)), C.byref(st)))
+    return out, {"closest_rays": st.closest_rays, "shadow_rays": st.shadow_rays}
+
+
 # --------------------------- synthetic workloads -----------------------------
 
 def gen_triangles(ctx: Context, n: int, seed: int, first: int = 0, half_extent: float = 0.01):

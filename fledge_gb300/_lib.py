@@ -55,6 +55,21 @@ class FlgTrCkpt(C.Structure):
     _fields_ = [("t", C.c_void_p), ("k", C.c_void_p), ("c", C.c_void_p)]
 
 
+class FlgPtScene(C.Structure):
+    _fields_ = [("pos", C.c_void_p), ("idx", C.c_void_p), ("n_tri", C.c_int64), ("n_vert", C.c_int64),
+                ("light_first", C.c_int32), ("light_count", C.c_int32), ("light_le", C.c_float * 3),
+                ("albedo", C.c_float * 3)]
+
+
+class FlgPtCamera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3), ("fov_deg", C.c_float),
+                ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class FlgPtStats(C.Structure):
+    _fields_ = [("closest_rays", C.c_int64), ("shadow_rays", C.c_int64)]
+
+
 P = C.c_void_p
 I32, I64, U32, U64, F32 = C.c_int32, C.c_int64, C.c_uint32, C.c_uint64, C.c_float
 PP = C.POINTER(C.c_void_p)
@@ -92,6 +107,8 @@ SIGNATURES = {
     "flg_volume_tr": [P, P, C.POINTER(FlgRays), I64, U64, P, C.POINTER(FlgTrCkpt)],
     "flg_volume_tr_adjoint": [P, P, C.POINTER(FlgRays), I64, U64, P, P, C.POINTER(FlgTrCkpt), P],
     "flg_volume_sample": [P, P, C.POINTER(FlgRays), I64, U64, P, P, P],
+    "flg_pathtrace": [P, P, C.POINTER(FlgPtScene), C.POINTER(FlgPtCamera), I32, I32, C.POINTER(FlgTraceOpts), P,
+                      C.POINTER(FlgPtStats)],
     "flg_graph_begin": [P],
     "flg_graph_end": [P, PP],
     "flg_graph_launch": [P, P],

@@ -108,6 +108,7 @@ FLG_API int flg_ctx_destroy(flg_ctx c) {
   cudaFree(c->d_work);
   cudaFree(c->d_ray_off);
   cudaFree(c->stage);
+  cudaFree(c->pt_buf);
   delete c;
   return FLG_OK;
 }

@@ -22,30 +22,6 @@ struct Cand {
   float lo[3], hi[3];
 };
 
-// Biased exponent e of the smallest power of two 2^(e-127) with
-// extent <= 255 * 2^(e-127) (with a little headroom); at least 1.
-__device__ __forceinline__ uint32_t quant_exponent(float extent) {
-  const float x = extent * (1.0f / 255.0f) * 1.00001f;
-  const uint32_t b = __float_as_uint(x);
-  uint32_t e = (b >> 23) & 0xFFu;
-  if (e == 0) return 1u;                    // zero or denormal extent
-  if (b & 0x7FFFFFu) ++e;                   // round up to a power of two
-  return e > 254u ? 254u : e;
-}
-
-// Outward-rounded 8-bit planes: decode(q) = org + q * s must not exceed the
-// exact lower plane (quant_down) nor fall below the exact upper plane.
-__device__ __forceinline__ uint8_t quant_down(float v, float org, float s) {
-  float q = fminf(fmaxf(floorf((v - org) / s), 0.0f), 255.0f);
-  while (q > 0.0f && fmaf(q, s, org) > v) q -= 1.0f;
-  return (uint8_t)q;
-}
-__device__ __forceinline__ uint8_t quant_up(float v, float org, float s) {
-  float q = fminf(fmaxf(ceilf((v - org) / s), 0.0f), 255.0f);
-  while (q < 255.0f && fmaf(q, s, org) < v) q += 1.0f;
-  return (uint8_t)q;
-}
-
 __device__ __forceinline__ float half_area(const Cand &c) {
   float dx = c.hi[0] - c.lo[0], dy = c.hi[1] - c.lo[1], dz = c.hi[2] - c.lo[2];
   return dx * dy + dy * dz + dz * dx;
@@ -123,33 +99,15 @@ __global__ void __launch_bounds__(128)
       ++nc;
     }
     NodeW<W> out;
-    // Quantisation frame: the union of the children, a power-of-two step
-    // per axis with the extent <= 255 steps.
-    float nlo[3], s[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      float lo = c[0].lo[a], hi = c[0].hi[a];
-#pragma unroll
-      for (int k = 1; k < W; ++k)
-        if (k < nc) {
-          lo = fminf(lo, c[k].lo[a]);
-          hi = fmaxf(hi, c[k].hi[a]);
-        }
-      nlo[a] = lo;
-      out.org[a] = lo;
-      const uint32_t e = quant_exponent(hi - lo);
-      out.ex[a] = (uint8_t)e;
-      s[a] = __uint_as_float(e << 23);
-    }
-    out.ex[3] = 0;
 #pragma unroll
     for (int k = 0; k < W; ++k) {
       if (k < nc) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          out.q[2 * a][k] = quant_down(c[k].lo[a], nlo[a], s[a]);
-          out.q[2 * a + 1][k] = quant_up(c[k].hi[a], nlo[a], s[a]);
-        }
+        out.lox[k] = c[k].lo[0];
+        out.loy[k] = c[k].lo[1];
+        out.loz[k] = c[k].lo[2];
+        out.hix[k] = c[k].hi[0];
+        out.hiy[k] = c[k].hi[1];
+        out.hiz[k] = c[k].hi[2];
         if (c[k].ref < 0 || c[k].count <= leaf_size) {
           out.child[k] = ~((c[k].first << 3) | (c[k].count - 1));
         } else {
@@ -164,8 +122,9 @@ __global__ void __launch_bounds__(128)
           }
         }
       } else {
-#pragma unroll
-        for (int a = 0; a < 6; ++a) out.q[a][k] = 0;
+        const float inf = __int_as_float(0x7f800000);
+        out.lox[k] = out.loy[k] = out.loz[k] = inf;
+        out.hix[k] = out.hiy[k] = out.hiz[k] = inf;
         out.child[k] = kEmptyChild;
       }
     }

@@ -23,25 +23,25 @@ struct alignas(16) Node2 {
   int4 d;    // child0, child1, parent (global, -1 root), scene
 };
 
-// Wide node of width W with quantised child boxes (after Ylitie, Karras and
-// Laine, "Efficient incoherent ray traversal on GPUs through compressed wide
-// BVHs", HPG 2017): the node's lower corner `org`, a power-of-two scale per
-// axis (biased exponent in `ex`), and per child and axis an 8-bit lower and
-// upper plane, rounded outward so every child box contains its exact box.
-// Rows q[0..5] are lo.x, hi.x, lo.y, hi.y, lo.z, hi.z, one byte per child.
-// Child refs: >= 0 wide node index; < 0 leaf range ~(first << 3 | (count-1))
-// over sorted triangles; kEmptyChild = unused slot (its box is inverted).
-// 64 bytes for W = 4, 96 bytes for W = 8 (4 / 6 16-byte loads per visit).
+// Bit pattern of a child box word not yet written by the refit: a NaN whose
+// payload min/max of vertex coordinates never produce (they return an input
+// or the canonical NaN).
+constexpr int32_t kBoxUnset = (int32_t)0xFFC0DEADu;
+
+// Wide node of width W, structure of arrays inside the record (7 / 14
+// 16-byte loads per visit).  Child refs: >= 0 wide node index; < 0 leaf range
+// ~(first << 3 | (count - 1)) over sorted triangles; kEmptyChild = unused
+// slot.  (8-bit quantised child boxes, 64 / 96 bytes, were measured too: no
+// gain on incoherent rays, 35 % slower on coherent camera rays, where the
+// decode's integer work dominates.)
 constexpr int32_t kEmptyChild = 0x7FFFFFFF;
 template <int W>
-struct alignas(W == 4 ? 64 : 32) NodeW {
-  float org[3];
-  uint8_t ex[4];
-  uint8_t q[6][W];
+struct alignas(16) NodeW {
+  float lox[W], hix[W], loy[W], hiy[W], loz[W], hiz[W];
   int32_t child[W];
 };
-static_assert(sizeof(NodeW<4>) == 64, "NodeW<4> layout");
-static_assert(sizeof(NodeW<8>) == 96, "NodeW<8> layout");
+static_assert(sizeof(NodeW<4>) == 112, "NodeW<4> layout");
+static_assert(sizeof(NodeW<8>) == 224, "NodeW<8> layout");
 
 // Sorted triangle record: v0.xyz + original (scene-local) id, v1, v2.
 struct alignas(16) TriRec {
@@ -73,6 +73,9 @@ struct flg_ctx_t {
   // Device staging buffers for flg_trace_closest_host (grown on demand).
   void *stage = nullptr;
   size_t stage_bytes = 0;
+  // Wavefront queues of flg_pathtrace (grown on demand).
+  void *pt_buf = nullptr;
+  size_t pt_bytes = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
@@ -183,5 +186,8 @@ int build_enqueue(flg_ctx ctx, flg_bvh b);
 int collapse_reserve(flg_ctx ctx, flg_bvh b);
 int collapse_enqueue(flg_ctx ctx, flg_bvh b, int width, int leaf_size);
 int sort_enqueue(flg_ctx ctx, flg_bvh b);
+int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_rays *rays, int64_t n,
+                  const flg_trace_opts *opts, const int64_t *ray_off_dev, int n_scenes, flg_hits *hits,
+                  uint8_t *occ);
 
 }  // namespace flg

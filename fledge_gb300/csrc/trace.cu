@@ -238,58 +238,27 @@ __device__ __forceinline__ void sort_keys(uint64_t (&k)[W]) {
   }
 }
 
-// Tests the W children of a quantised wide node (4 or 6 16-byte loads).  Per
-// axis a child plane is t = q * (s / d) + (org - o) / d with one FMA; the near
-// and far values come from min/max (a NaN slab, 0 * inf, constrains nothing),
-// and the interval is widened by 2^-20 relative so that rounding never
-// rejects a box that contains a hit.  Returns the number of children hit with
-// tnear <= lim; their keys (tnear | ref) are in key[], misses are ~0.
+// Tests the W children of a wide node (7 / 14 16-byte loads) with the
+// reference's slab test (slab_tnear).  Returns the number of children hit
+// with tnear <= lim; their keys (tnear | ref) are in key[], misses are ~0.
 template <int W>
 __device__ __forceinline__ int visit_node(const NodeW<W> *__restrict__ node, const float3 &o, const float3 &inv,
                                           float lim, uint64_t (&key)[W]) {
-  constexpr int NV = (int)sizeof(NodeW<W>) / 16;
-  constexpr int RW = W / 4;  // 32-bit words per quantised row
-  uint32_t u[4 * NV];
-  const uint4 *np = (const uint4 *)node;
+  constexpr int NV = 7 * W / 4;
+  float f[4 * NV];
+  const float4 *np = (const float4 *)node;
 #pragma unroll
   for (int k = 0; k < NV; ++k) {
-    const uint4 q = __ldg(np + k);
-    u[4 * k] = q.x; u[4 * k + 1] = q.y; u[4 * k + 2] = q.z; u[4 * k + 3] = q.w;
+    const float4 q = __ldg(np + k);
+    f[4 * k] = q.x; f[4 * k + 1] = q.y; f[4 * k + 2] = q.z; f[4 * k + 3] = q.w;
   }
-  const float sx = __uint_as_float((u[3] & 0xFFu) << 23) * inv.x;
-  const float sy = __uint_as_float(((u[3] >> 8) & 0xFFu) << 23) * inv.y;
-  const float sz = __uint_as_float(((u[3] >> 16) & 0xFFu) << 23) * inv.z;
-  const float bx = (__uint_as_float(u[0]) - o.x) * inv.x;
-  const float by = (__uint_as_float(u[1]) - o.y) * inv.y;
-  const float bz = (__uint_as_float(u[2]) - o.z) * inv.z;
-  // Near and far plane rows per axis from the ray's direction signs (one
-  // select per packed word instead of a min/max per child and axis).
-  uint32_t nw[3][RW], fw[3][RW];
-  const bool neg[3] = {inv.x < 0.0f, inv.y < 0.0f, inv.z < 0.0f};
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int r = 0; r < RW; ++r) {
-      const uint32_t lo = u[4 + (2 * a) * RW + r], hi = u[4 + (2 * a + 1) * RW + r];
-      nw[a][r] = neg[a] ? hi : lo;
-      fw[a][r] = neg[a] ? lo : hi;
-    }
   int nh = 0;
 #pragma unroll
   for (int k = 0; k < W; ++k) {
-    const int32_t ref = (int32_t)u[4 + 6 * RW + k];
-    // byte k of a row word -> float: 0x4B0000qq is 2^23 + q exactly
-    const uint32_t sel = 0x7540u | (uint32_t)(k & 3);
-    const float qnx = __uint_as_float(__byte_perm(nw[0][k / 4], 0x4B000000u, sel)) - 8388608.0f;
-    const float qfx = __uint_as_float(__byte_perm(fw[0][k / 4], 0x4B000000u, sel)) - 8388608.0f;
-    const float qny = __uint_as_float(__byte_perm(nw[1][k / 4], 0x4B000000u, sel)) - 8388608.0f;
-    const float qfy = __uint_as_float(__byte_perm(fw[1][k / 4], 0x4B000000u, sel)) - 8388608.0f;
-    const float qnz = __uint_as_float(__byte_perm(nw[2][k / 4], 0x4B000000u, sel)) - 8388608.0f;
-    const float qfz = __uint_as_float(__byte_perm(fw[2][k / 4], 0x4B000000u, sel)) - 8388608.0f;
-    const float tn = fmaxf(fmaxf(fmaf(qnx, sx, bx), fmaf(qny, sy, by)), fmaxf(fmaf(qnz, sz, bz), 0.0f));
-    const float tf = fminf(fminf(fmaf(qfx, sx, bx), fmaf(qfy, sy, by)), fminf(fmaf(qfz, sz, bz), lim));
-    const bool ok = ref != kEmptyChild && tn * 0.99999905f <= tf * 1.00000095f;
-    key[k] = ok ? stack_key(tn, ref) : ~0ull;
+    const int32_t ref = __float_as_int(f[6 * W + k]);
+    const float t = slab_tnear(f[k], f[W + k], f[2 * W + k], f[3 * W + k], f[4 * W + k], f[5 * W + k], o, inv);
+    const bool ok = ref != kEmptyChild && t <= lim;
+    key[k] = ok ? stack_key(t, ref) : ~0ull;
     nh += ok ? 1 : 0;
   }
   return nh;

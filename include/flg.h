@@ -265,6 +265,41 @@ FLG_API int flg_volume_tr_adjoint(flg_ctx ctx, flg_grid grid, const flg_rays *ra
 FLG_API int flg_volume_sample(flg_ctx ctx, flg_grid grid, const flg_rays *rays, int64_t n,
                               uint64_t seed, uint8_t *success, float *p, float *weight);
 
+/* ---------------------------- path tracing ------------------------------ */
+
+/* The integrator around traversal: PathIntegrator::Li (integrator.cpp:252-326)
+ * with one-light next-event estimation (:69-120) over a triangle mesh whose
+ * triangles [light_first, light_first + light_count) emit light_le (front
+ * side, geometric normal (p1-p0) x (p2-p0)); every other triangle is
+ * Lambertian with `albedo`.  Halton samples (sampler.h:143-252) in the
+ * per-pixel order of integrator.cpp:136-159; camera as Camera (camera.h). */
+typedef struct flg_pt_scene {
+  const float *pos;        /* device, 3 * n_vert */
+  const int32_t *idx;      /* device, 3 * n_tri, or NULL for a soup */
+  int64_t n_tri, n_vert;
+  int32_t light_first, light_count;
+  float light_le[3];
+  float albedo[3];
+} flg_pt_scene;
+
+typedef struct flg_pt_camera {
+  float eye[3], target[3], up[3];
+  float fov_deg;           /* Camera::m_fov (camera.h:25) */
+  int32_t width, height;
+} flg_pt_camera;
+
+typedef struct flg_pt_stats {
+  int64_t closest_rays, shadow_rays;  /* rays traced, all bounces and samples */
+} flg_pt_stats;
+
+/* Renders the image into radiance (device, 3 floats per pixel, row-major,
+ * mean over spp) as a wavefront: camera rays, closest hit, shading with
+ * queue compaction, shadow rays with any hit, per bounce.  bvh must be built
+ * over the same mesh.  Synchronises once per bounce. */
+FLG_API int flg_pathtrace(flg_ctx ctx, flg_bvh bvh, const flg_pt_scene *scene, const flg_pt_camera *cam,
+                          int32_t spp, int32_t max_depth, const flg_trace_opts *opts, float *radiance,
+                          flg_pt_stats *stats);
+
 /* ----------------------------- CUDA graphs ------------------------------ */
 
 /* Captures every library call issued on ctx between begin and end into a

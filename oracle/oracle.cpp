@@ -1129,3 +1129,261 @@ ORC_API int64_t orc_build(const float *pos, const int32_t *idx, int64_t n_tri, u
   orc_refit(pos, idx, n_tri, perm, split, leaf, parent, leaf_parent, nb);
   return n_tri - 1;
 }
+
+// ------------------------------ path tracing --------------------------------
+// PathIntegrator::Li (integrator.cpp:252-326) with UniformSampleOneLight /
+// EstimateDirect (:69-120), the Halton sampler (sampler.h:143-252) and
+// eval_pixel's sample order (integrator.cpp:136-159), over the oracle's
+// closest-hit (DEV arithmetic, refined hit values) and any-hit traversal.
+// Emitters: triangles [light_first, light_first + light_count); a light
+// triangle is chosen uniformly and sampled with UniformSampleTriangle
+// (math_utils.h:90-93) since the reference's Triangle::sample is TODO.
+namespace {
+
+const int kPrimes[64] = {2,   3,   5,   7,   11,  13,  17,  19,  23,  29,  31,  37,  41,  43,  47,  53,
+                         59,  61,  67,  71,  73,  79,  83,  89,  97,  101, 103, 107, 109, 113, 127, 131,
+                         137, 139, 149, 151, 157, 163, 167, 173, 179, 181, 191, 193, 197, 199, 211, 223,
+                         227, 229, 233, 239, 241, 251, 257, 263, 269, 271, 277, 281, 283, 293, 307, 311};
+
+float radical_inverse(int base, uint64_t a) {  // RadicalInverse_ (sampler.h)
+  const float inv_base = 1.0f / (float)base;
+  uint64_t rev = 0;
+  float inv_n = 1.0f;
+  while (a) {
+    uint64_t next = a / (uint64_t)base;
+    uint64_t digit = a - next * (uint64_t)base;
+    rev = rev * (uint64_t)base + digit;
+    inv_n *= inv_base;
+    a = next;
+  }
+  return (float)rev * inv_n;
+}
+
+uint64_t inverse_radical_inverse(int base, uint64_t inverse, int n_digits) {
+  uint64_t index = 0;
+  for (int i = 0; i < n_digits; ++i) {
+    uint64_t digit = inverse % (uint64_t)base;
+    inverse /= (uint64_t)base;
+    index = index * (uint64_t)base + digit;
+  }
+  return index;
+}
+
+struct HaltonH {
+  uint64_t scale[2], stride, inv[2];
+  int exp[2];
+  HaltonH(int w, int h) {  // HaltonSampler(SPP, {resX, resY}), M_MAX_RESOLUTION 128
+    const int res[2] = {w, h};
+    for (int i = 0; i < 2; ++i) {
+      const int base = i == 0 ? 2 : 3;
+      uint64_t sc = 1;
+      int e = 0;
+      while (sc < (uint64_t)std::min(res[i], 128)) {
+        sc *= base;
+        ++e;
+      }
+      scale[i] = sc;
+      exp[i] = e;
+    }
+    stride = scale[0] * scale[1];
+    inv[0] = mulinv((int64_t)scale[1], (int64_t)scale[0]);
+    inv[1] = mulinv((int64_t)scale[0], (int64_t)scale[1]);
+  }
+  static void exgcd(int64_t a, int64_t b, int64_t &x, int64_t &y) {  // ExGCD (sampler.h)
+    if (b == 0) {
+      x = 1;
+      y = 0;
+      return;
+    }
+    exgcd(b, a % b, y, x);
+    y -= a / b * x;
+  }
+  static uint64_t mulinv(int64_t a, int64_t b) {
+    int64_t x, y;
+    exgcd(a, b, x, y);
+    int64_t m = x % b;
+    return (uint64_t)(m < 0 ? m + b : m);
+  }
+  uint64_t offset(int x, int y) const {  // getIndexForSample
+    if (stride <= 1) return 0;
+    uint64_t off = inverse_radical_inverse(2, (uint64_t)(x % 128), exp[0]) * (stride / scale[0]) * inv[0];
+    off += inverse_radical_inverse(3, (uint64_t)(y % 128), exp[1]) * (stride / scale[1]) * inv[1];
+    return off % stride;
+  }
+  float sample(uint64_t index, int dim) const {  // sampleDimension + get1D clamp
+    float v;
+    if (dim == 0) v = radical_inverse(2, index / scale[0]);
+    else if (dim == 1) v = radical_inverse(3, index / scale[1]);
+    else v = radical_inverse(kPrimes[dim < 64 ? dim : 63], index);
+    return std::min(v, 0.99999994f);
+  }
+};
+
+inline V3 v3(float x, float y, float z) { return {x, y, z}; }
+inline V3 scale3(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+inline V3 norm3(V3 a) {
+  float l = std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+  return {a.x / l, a.y / l, a.z / l};
+}
+
+float offset_axis(float p, float off) {  // OffsetRayOrigin (common/ray.h:64-93)
+  int oi = (int)(off * 256.0f);
+  int pb;
+  std::memcpy(&pb, &p, 4);
+  pb += p < 0.0f ? -oi : oi;
+  float pi;
+  std::memcpy(&pi, &pb, 4);
+  return std::fabs(p) < (1.0f / 32.0f) ? p + (1.0f / 65536.0f) * off : pi;
+}
+V3 offset_origin(V3 p, V3 n, V3 d) {
+  V3 off = dot(n, d) <= 0.0f ? v3(-n.x, -n.y, -n.z) : n;
+  return {offset_axis(p.x, off.x), offset_axis(p.y, off.y), offset_axis(p.z, off.z)};
+}
+
+}  // namespace
+
+ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, const int32_t *perm,
+                           const int32_t *split, const uint8_t *leaf, const float *nb, int32_t light_first,
+                           int32_t light_count, const float *le, const float *albedo, const float *eye,
+                           const float *target, const float *up, float fov_deg, int32_t width, int32_t height,
+                           int32_t spp, int32_t max_depth, int32_t pixel_stride, float *radiance,
+                           int64_t *rays) {
+  Mesh M{pos, idx, n_tri};
+  Tree T{n_tri, perm, split, leaf, nb};
+  HaltonH H(width, height);
+  float f[3] = {target[0] - eye[0], target[1] - eye[1], target[2] - eye[2]};
+  auto nrm = [](float *v) {
+    const float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    v[0] /= l; v[1] /= l; v[2] /= l;
+  };
+  nrm(f);
+  float r[3] = {up[1] * f[2] - up[2] * f[1], up[2] * f[0] - up[0] * f[2], up[0] * f[1] - up[1] * f[0]};
+  nrm(r);
+  float u3[3] = {f[1] * r[2] - f[2] * r[1], f[2] * r[0] - f[0] * r[2], f[0] * r[1] - f[1] * r[0]};
+  nrm(u3);
+  const float fov_ratio = std::tan(3.14159265358979f * fov_deg / 360.0f);
+  const float aspect = (float)width / (float)height;
+  const float inv_spp = 1.0f / (float)spp;
+  int64_t n_closest = 0, n_shadow = 0;
+  const int64_t npix = (int64_t)width * height;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : n_closest, n_shadow)
+  for (int64_t pix = 0; pix < npix; pix += pixel_stride) {
+    const int x = (int)(pix % width), y = (int)(pix / width);
+    const uint64_t off = H.offset(x, y);
+    double acc[3] = {0.0, 0.0, 0.0};
+    int cnt_end0 = 0;
+    for (int s = 0; s < spp; ++s) {
+      float px, py;
+      int cnt;
+      uint64_t index = off + (uint64_t)(s > 0 ? s - 1 : 0) * H.stride;
+      if (s == 0) {
+        px = (float)x + 0.5f;
+        py = (float)y + 0.5f;
+        cnt = 0;
+      } else {
+        cnt = s == 1 ? cnt_end0 : 0;
+        px = (float)x + H.sample(index, cnt);
+        py = (float)y + H.sample(index, cnt + 1);
+        cnt += 2;
+      }
+      // Camera::generateRay (camera.h:22-31)
+      const float yo = fov_ratio * ((py / (float)height) * 2.0f - 1.0f);
+      const float xo = fov_ratio * aspect * ((px / (float)width) * 2.0f - 1.0f);
+      V3 O = v3(eye[0], eye[1], eye[2]);
+      V3 D = norm3(v3(f[0] + xo * r[0] + yo * u3[0], f[1] + xo * r[1] + yo * u3[1], f[2] + xo * r[2] + yo * u3[2]));
+      float beta[3] = {1.0f, 1.0f, 1.0f};
+      for (int depth = 0;; ++depth) {
+        RayIn ray;
+        ray.o[0] = O.x; ray.o[1] = O.y; ray.o[2] = O.z;
+        ray.d[0] = D.x; ray.d[1] = D.y; ray.d[2] = D.z;
+        for (int k = 0; k < 3; ++k) ray.inv[k] = 1.0f / ray.d[k];
+        ray.tmin = 1e-30f;
+        ray.tmax = 3.402823466e+38f;
+        Best b{ray.tmax, -1, 0.0f, 0.0f};
+        recursive_intersect(T, M, 0, ray, MODE_DEV, b);
+        ++n_closest;
+        if (b.prim >= 0) refine_tuv(M.v(b.prim, 0), M.v(b.prim, 1), M.v(b.prim, 2), ray.o, ray.d, b.tfar, b.u, b.v);
+        if (b.prim < 0) break;
+        const V3 a = ld3(M.v(b.prim, 0)), bb = ld3(M.v(b.prim, 1)), c = ld3(M.v(b.prim, 2));
+        const float w = 1.0f - b.u - b.v;
+        const V3 p = v3(w * a.x + b.u * bb.x + b.v * c.x, w * a.y + b.u * bb.y + b.v * c.y,
+                        w * a.z + b.u * bb.z + b.v * c.z);
+        const V3 ng = norm3(cross(sub(bb, a), sub(c, a)));
+        const bool is_light = b.prim >= light_first && b.prim < light_first + light_count;
+        if (depth == 0 && is_light && dot(ng, v3(-D.x, -D.y, -D.z)) > 0.0f)
+          for (int k = 0; k < 3; ++k) acc[k] += (double)(beta[k] * le[k] * inv_spp);
+        if (depth >= max_depth) break;
+        const float ul = H.sample(index, cnt), ua = H.sample(index, cnt + 1), ub = H.sample(index, cnt + 2);
+        cnt += 3;
+        const int li = std::min((int)(ul * (float)light_count), light_count - 1);
+        const float light_pdf = 1.0f / (float)light_count;
+        const int64_t lt = light_first + li;
+        const V3 la = ld3(M.v(lt, 0)), lb = ld3(M.v(lt, 1)), lc = ld3(M.v(lt, 2));
+        const float su0 = std::sqrt(ua);
+        const float b0 = 1.0f - su0, b1 = ub * su0, b2 = 1.0f - b0 - b1;
+        const V3 lp = v3(b0 * la.x + b1 * lb.x + b2 * lc.x, b0 * la.y + b1 * lb.y + b2 * lc.y,
+                         b0 * la.z + b1 * lb.z + b2 * lc.z);
+        const V3 lcr = cross(sub(lb, la), sub(lc, la));
+        const float area = 0.5f * std::sqrt(dot(lcr, lcr));
+        const V3 ln = scale3(lcr, 1.0f / (2.0f * area));
+        const V3 toL = sub(lp, p);
+        const float dist = std::sqrt(dot(toL, toL));
+        const V3 wi = scale3(toL, 1.0f / dist);
+        const float cos_l = -dot(ln, wi);
+        if (cos_l > 0.0f && dist > 0.0f) {
+          const float pdf = dist * dist / (cos_l * area);
+          const float cos_s = std::fabs(dot(wi, ng));
+          const float k = cos_s * (1.0f / 3.14159265358979f) / (pdf * light_pdf) * inv_spp;
+          const float ct[3] = {beta[0] * albedo[0] * le[0] * k, beta[1] * albedo[1] * le[1] * k,
+                               beta[2] * albedo[2] * le[2] * k};
+          if (ct[0] > 0.0f || ct[1] > 0.0f || ct[2] > 0.0f) {
+            const V3 so = offset_origin(p, ng, wi);
+            RayIn sr;
+            sr.o[0] = so.x; sr.o[1] = so.y; sr.o[2] = so.z;
+            sr.d[0] = wi.x; sr.d[1] = wi.y; sr.d[2] = wi.z;
+            for (int q = 0; q < 3; ++q) sr.inv[q] = 1.0f / sr.d[q];
+            sr.tmin = 1e-30f;
+            sr.tmax = dist - 1e-4f;
+            ++n_shadow;
+            if (!recursive_occluded(T, M, 0, sr, MODE_DEV))
+              for (int q = 0; q < 3; ++q) acc[q] += (double)ct[q];
+          }
+        }
+        const float u1 = H.sample(index, cnt), u2 = H.sample(index, cnt + 1);
+        cnt += 2;
+        V3 bn = std::fabs(ng.x) > std::fabs(ng.z) ? v3(-ng.y, ng.x, 0.0f) : v3(0.0f, -ng.z, ng.y);
+        bn = norm3(bn);
+        const V3 tg = cross(bn, ng);
+        const float woz = dot(v3(-D.x, -D.y, -D.z), ng);
+        const float ux = u1 * 2.0f - 1.0f, uy = u2 * 2.0f - 1.0f;
+        float dx = 0.0f, dy = 0.0f;
+        if (ux != 0.0f || uy != 0.0f) {
+          float rr, th;
+          if (std::fabs(ux) > std::fabs(uy)) {
+            rr = ux;
+            th = 0.78539816f * (uy / ux);
+          } else {
+            rr = uy;
+            th = 1.57079633f - 0.78539816f * (ux / uy);
+          }
+          dx = std::cos(th) * rr;
+          dy = std::sin(th) * rr;
+        }
+        const float dz = std::sqrt(std::max(0.0f, 1.0f - dx * dx - dy * dy));
+        const float pdf_b = woz * dz > 0.0f ? std::fabs(dz) * (1.0f / 3.14159265358979f) : 0.0f;
+        if (!(pdf_b > 0.0f)) break;
+        V3 nd = v3(tg.x * dx + bn.x * dy + ng.x * dz, tg.y * dx + bn.y * dy + ng.y * dz,
+                   tg.z * dx + bn.z * dy + ng.z * dz);
+        const float fcos = (1.0f / 3.14159265358979f) * std::fabs(dot(nd, ng)) / pdf_b;
+        for (int q = 0; q < 3; ++q) beta[q] = beta[q] * albedo[q] * fcos;
+        nd = norm3(nd);
+        O = offset_origin(p, ng, nd);
+        D = nd;
+      }
+      if (s == 0) cnt_end0 = cnt;
+    }
+    for (int k = 0; k < 3; ++k) radiance[3 * pix + k] = (float)acc[k];
+  }
+  rays[0] = n_closest;
+  rays[1] = n_shadow;
+}
