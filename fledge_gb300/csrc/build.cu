@@ -10,10 +10,12 @@
 //   3. sort            onesweep radix sort (sort.cu)
 //   4. k_karras        one thread per internal node: direction, range, split
 //                      (radix_bvh.cpp:118-161) and child/parent links
-//   5. k_refit         one thread per leaf: gathers its triangle into the
-//                      sorted triangle array, then climbs with per-node
+//   5. k_refit         lanes over sorted leaves: gather the triangle into the
+//                      sorted triangle array, then climb with per-node
 //                      arrival counters (radix_bvh.cpp:163-199); each child
-//                      box is written once, into its parent's record
+//                      box is written once, into its parent's record, and
+//                      the second arrival polls for its sibling's box (no
+//                      fence per level)
 //   6. (optional) collapse to 4- or 8-wide nodes (collapse.cu)
 #include <cuda/atomic>
 
@@ -183,7 +185,8 @@ __global__ void __launch_bounds__(256)
     k_karras(const uint32_t *__restrict__ keys, const int64_t *__restrict__ tri_off,
              const int64_t *__restrict__ node_off, int n_scenes, int64_t n_nodes,
              int32_t *__restrict__ split_o, uint8_t *__restrict__ leaf_o, int32_t *__restrict__ range_o,
-             int32_t *__restrict__ parent_o, int32_t *__restrict__ leaf_parent_o, Node2 *__restrict__ nodes) {
+             int32_t *__restrict__ parent_o, int32_t *__restrict__ leaf_parent_o, Node2 *__restrict__ nodes,
+             uint32_t *__restrict__ flags_o) {
   for (int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gi < n_nodes;
        gi += (int64_t)gridDim.x * blockDim.x) {
     const int s = find_segment(node_off, n_scenes, gi);
@@ -212,105 +215,172 @@ __global__ void __launch_bounds__(256)
     split_o[gi] = split;
     leaf_o[gi] = lf;
     range_o[gi] = j;
+    // Parent links carry the child's side in bit 0 (0: the child at split,
+    // 1: the child at split + 1), so the refit climb needs one load a level.
     int c0, c1;
     if (lf & 1) {
       c0 = ~(int)(toff + split);
-      leaf_parent_o[toff + split] = i;
+      leaf_parent_o[toff + split] = i << 1;
     } else {
       c0 = (int)(noff + split);
-      parent_o[noff + split] = i;
+      parent_o[noff + split] = i << 1;
       nodes[noff + split].d.z = (int)gi;
     }
     if (lf & 2) {
       c1 = ~(int)(toff + split + 1);
-      leaf_parent_o[toff + split + 1] = i;
+      leaf_parent_o[toff + split + 1] = (i << 1) | 1;
     } else {
       c1 = (int)(noff + split + 1);
-      parent_o[noff + split + 1] = i;
+      parent_o[noff + split + 1] = (i << 1) | 1;
       nodes[noff + split + 1].d.z = (int)gi;
     }
+    // Child boxes start as the "not yet written" pattern the refit polls on.
+    const float u = __int_as_float(kBoxUnset);
+    float4 *f4 = (float4 *)(nodes + gi);
+    f4[0] = f4[1] = f4[2] = make_float4(u, u, u, u);
     nodes[gi].d.x = c0;
     nodes[gi].d.y = c1;
     nodes[gi].d.w = s;
-    if (i == 0) nodes[gi].d.z = -1;
+    flags_o[gi] = 0u;
+    if (i == 0) {
+      nodes[gi].d.z = -1;
+      parent_o[gi] = 0;
+    }
   }
 }
 
 // Child box of side s lives in float4 s (x/y lo-hi) and float2 s of the third
-// float4 (z lo-hi): one 16-byte and one 8-byte access each way.
+// float4 (z lo-hi).  Stores and polls are relaxed device-scope accesses: the
+// climb orders nothing else through them, so no fence is needed.
 __device__ __forceinline__ void store_child_box(Node2 *nd, int side, const float *lo, const float *hi) {
   float4 *f4 = (float4 *)nd;
   float2 *f2 = (float2 *)(f4 + 2);
-  __stcg(f4 + side, make_float4(lo[0], hi[0], lo[1], hi[1]));
-  __stcg(f2 + side, make_float2(lo[2], hi[2]));
-}
-__device__ __forceinline__ void load_child_box(const Node2 *nd, int side, float *lo, float *hi) {
-  const float4 *f4 = (const float4 *)nd;
-  const float2 *f2 = (const float2 *)(f4 + 2);
-  const float4 a = __ldcg(f4 + side);
-  const float2 z = __ldcg(f2 + side);
-  lo[0] = a.x; hi[0] = a.y; lo[1] = a.z; hi[1] = a.w;
-  lo[2] = z.x; hi[2] = z.y;
+  asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(f4 + side), "f"(lo[0]), "f"(hi[0]),
+               "f"(lo[1]), "f"(hi[1])
+               : "memory");
+  asm volatile("st.relaxed.gpu.global.v2.f32 [%0], {%1, %2};" ::"l"(f2 + side), "f"(lo[2]), "f"(hi[2]) : "memory");
 }
 
-// One thread per sorted leaf: gather the triangle, then climb.  The first
-// child to arrive at a node stops; the second merges its sibling's box (read
-// from L2 after the arrival counter) and continues (radix_bvh.cpp:163-199).
+// One relaxed read of a child box; true when none of its six words holds
+// kBoxUnset any more.  Each word is written once, so per-word coherence is
+// all the polling relies on (no fence orders the sibling's stores).
+__device__ __forceinline__ bool read_child_box(const Node2 *nd, int side, float *lo, float *hi) {
+  const float4 *f4 = (const float4 *)nd;
+  const float2 *f2 = (const float2 *)(f4 + 2);
+  float a0, a1, a2, a3, z0, z1;
+  asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(a0), "=f"(a1), "=f"(a2), "=f"(a3)
+               : "l"(f4 + side)
+               : "memory");
+  asm volatile("ld.relaxed.gpu.global.v2.f32 {%0, %1}, [%2];" : "=f"(z0), "=f"(z1) : "l"(f2 + side) : "memory");
+  lo[0] = a0; hi[0] = a1; lo[1] = a2; hi[1] = a3; lo[2] = z0; hi[2] = z1;
+  return __float_as_int(a0) != kBoxUnset && __float_as_int(a1) != kBoxUnset && __float_as_int(a2) != kBoxUnset &&
+         __float_as_int(a3) != kBoxUnset && __float_as_int(z0) != kBoxUnset && __float_as_int(z1) != kBoxUnset;
+}
+
+// Polls until read_child_box succeeds; false after `limit` polls.
+__device__ __forceinline__ bool wait_child_box(const Node2 *nd, int side, float *lo, float *hi, uint32_t limit) {
+  for (uint32_t spins = 0;; ++spins) {
+    if (read_child_box(nd, side, lo, hi)) return true;
+    if (spins >= limit) return false;
+    if (spins > 16) __nanosleep(32);
+  }
+}
+
+// Bottom-up refit (radix_bvh.cpp:163-199).  Each warp owns a contiguous
+// chunk of sorted leaves.  A lane gathers its leaf's triangle into the sorted
+// triangle array, then climbs: at every node it writes its own box into the
+// parent's record and counts its arrival; the first arrival stops, the second
+// waits for the sibling's box, merges and goes on up.  Lanes that stopped
+// take new leaves together, once half the warp is idle, so that the gathers
+// of a refill run side by side on consecutive leaves.
+constexpr int kRefitRefill = 16;
+
 __global__ void __launch_bounds__(256)
     k_refit(const float *__restrict__ pos, const int32_t *__restrict__ idx, int64_t n_tri,
             const int64_t *__restrict__ tri_off, const int64_t *__restrict__ node_off, int n_scenes,
-            const uint32_t *__restrict__ perm, const int32_t *__restrict__ split,
-            const int32_t *__restrict__ parent, const int32_t *__restrict__ leaf_parent, Node2 *nodes,
-            uint32_t *flags, TriRec *__restrict__ tris, uint32_t *err) {
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n_tri;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    const int s = find_segment(tri_off, n_scenes, g);
-    const int64_t toff = tri_off[s], noff = node_off[s];
-    const int n = (int)(tri_off[s + 1] - toff);
-    const int li = (int)(g - toff);
-    const int64_t orig = perm[g];
-    // A sort that timed out leaves unspecified slots: never follow them.
-    if (orig < toff || orig >= toff + n) {
-      atomicOr(err, kErrTimeout);
-      continue;
+            const uint32_t *__restrict__ perm, const int32_t *__restrict__ parent,
+            const int32_t *__restrict__ leaf_parent, Node2 *nodes, uint32_t *flags, TriRec *__restrict__ tris,
+            uint32_t spin_limit, uint32_t *err) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt = (1u << lane) - 1u;
+  const int64_t n_warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t chunk = (n_tri + n_warps - 1) / n_warps;
+  int64_t next = warp * chunk;
+  const int64_t end = min(next + chunk, n_tri);
+  bool climbing = false;
+  int cur = 0, side = 0, n = 0, depth = 0;
+  int64_t noff = 0;
+  float lo[3], hi[3];
+  for (;;) {
+    const unsigned idle = __ballot_sync(0xFFFFFFFFu, !climbing);
+    const int nidle = __popc(idle);
+    if (next < end && nidle >= kRefitRefill) {
+      const int64_t leaf = next + __popc(idle & lt);
+      next += nidle;
+      if (!climbing && leaf < end) {
+        const int s = find_segment(tri_off, n_scenes, leaf);
+        const int64_t toff = tri_off[s];
+        noff = node_off[s];
+        n = (int)(tri_off[s + 1] - toff);
+        const int64_t orig = perm[leaf];
+        // A sort that timed out leaves unspecified slots: never follow them.
+        if (orig < toff || orig >= toff + n) {
+          atomicOr(err, kErrTimeout);
+        } else {
+          float3 p0, p1, p2;
+          tri_verts(pos, idx, orig, p0, p1, p2);
+          TriRec r;
+          r.p0 = make_float4(p0.x, p0.y, p0.z, __int_as_float((int)(orig - toff)));
+          r.p1 = make_float4(p1.x, p1.y, p1.z, 0.0f);
+          r.p2 = make_float4(p2.x, p2.y, p2.z, 0.0f);
+          tris[leaf] = r;
+          if (n >= 2) {
+            tri_box(p0, p1, p2, lo, hi);
+            const int ps = leaf_parent[leaf];
+            cur = ps >> 1;
+            side = ps & 1;
+            depth = 0;
+            climbing = true;
+          }
+        }
+      }
+    } else if (nidle == 32) {
+      break;  // every leaf of the chunk taken and every climb finished
     }
-    float3 p0, p1, p2;
-    tri_verts(pos, idx, orig, p0, p1, p2);
-    TriRec r;
-    r.p0 = make_float4(p0.x, p0.y, p0.z, __int_as_float((int)(orig - toff)));
-    r.p1 = make_float4(p1.x, p1.y, p1.z, 0.0f);
-    r.p2 = make_float4(p2.x, p2.y, p2.z, 0.0f);
-    tris[g] = r;
-    if (n < 2) continue;
-    float lo[3], hi[3];
-    tri_box(p0, p1, p2, lo, hi);
-    int cur = leaf_parent[g];
-    int side = (li == split[noff + cur]) ? 0 : 1;
+    if (!climbing) continue;
     // A valid Karras tree is at most 30 + 32 levels deep; the bound only
     // matters if the inputs were corrupted by an earlier timed-out wait.
-    for (int depth = 0;; ++depth) {
-      if (depth > 96 || cur < 0 || cur >= n - 1) {
-        atomicOr(err, kErrTimeout);
-        break;
-      }
-      Node2 *nd = nodes + noff + cur;
-      store_child_box(nd, side, lo, hi);
-      // Release: the box above is visible before the count; acquire: the
-      // sibling's box, published before its increment, is read after ours.
-      cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrival(flags[noff + cur]);
-      const uint32_t old = arrival.fetch_add(1u, cuda::memory_order_acq_rel);
-      if (old == 0u) break;
-      float olo[3], ohi[3];
-      load_child_box(nd, side ^ 1, olo, ohi);
-      for (int k = 0; k < 3; ++k) {
-        lo[k] = fminf(lo[k], olo[k]);
-        hi[k] = fmaxf(hi[k], ohi[k]);
-      }
-      if (cur == 0) break;
-      int p = parent[noff + cur];
-      side = (cur == split[noff + p]) ? 0 : 1;
-      cur = p;
+    if (depth > 96 || cur < 0 || cur >= n - 1) {
+      atomicOr(err, kErrTimeout);
+      climbing = false;
+      continue;
     }
+    Node2 *nd = nodes + noff + cur;
+    store_child_box(nd, side, lo, hi);
+    const int ps = parent[noff + cur];  // in flight with the arrival count
+    if (atomicAdd(flags + noff + cur, 1u) == 0u) {
+      climbing = false;
+      continue;
+    }
+    float olo[3], ohi[3];
+    if (!wait_child_box(nd, side ^ 1, olo, ohi, spin_limit)) {
+      atomicOr(err, kErrTimeout);
+      climbing = false;
+      continue;
+    }
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = fminf(lo[k], olo[k]);
+      hi[k] = fmaxf(hi[k], ohi[k]);
+    }
+    if (cur == 0) {
+      climbing = false;
+      continue;
+    }
+    cur = ps >> 1;
+    side = ps & 1;
+    ++depth;
   }
 }
 
@@ -335,8 +405,6 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
                                 sizeof(uint32_t) * 256 * (size_t)b->n_tiles * b->n_passes, st));
   FLG_CUDA(ctx, cudaMemsetAsync(b->d_tile_ctr, 0, sizeof(uint32_t) * b->n_passes, st));
   if (b->n_nodes > 0) {
-    FLG_CUDA(ctx, cudaMemsetAsync(b->d_flags, 0, sizeof(uint32_t) * b->n_nodes, st));
-    FLG_CUDA(ctx, cudaMemsetAsync(b->d_parent, 0, sizeof(int32_t) * b->n_nodes, st));
   }
 
   k_scene_bounds<<<grid_for(n, kBoundsChunk), kBoundsThreads, 0, st>>>(b->pos, b->idx, n, b->d_tri_off,
@@ -352,12 +420,19 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
   if (b->n_nodes > 0) {
     k_karras<<<grid_for(b->n_nodes, 256, (int64_t)ctx->num_sms * 16), 256, 0, st>>>(
         b->d_keys, b->d_tri_off, b->d_node_off, b->n_scenes, b->n_nodes, b->d_split, b->d_leaf,
-        b->d_range_j, b->d_parent, b->d_leaf_parent, b->d_nodes2);
+        b->d_range_j, b->d_parent, b->d_leaf_parent, b->d_nodes2, b->d_flags);
     FLG_LAUNCH_CHECK(ctx, "k_karras");
   }
-  k_refit<<<grid_for(n, 256, (int64_t)ctx->num_sms * 16), 256, 0, st>>>(
-      b->pos, b->idx, n, b->d_tri_off, b->d_node_off, b->n_scenes, b->d_perm, b->d_split, b->d_parent,
-      b->d_leaf_parent, b->d_nodes2, b->d_flags, b->d_tris, ctx->d_err);
+  // Lanes take their next leaf as soon as they stop climbing, so one wave
+  // of resident CTAs balances better than more CTAs than fit.
+  static const int refit_per_sm = [] {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_refit, 256, 0) != cudaSuccess || v < 1) v = 1;
+    return v;
+  }();
+  k_refit<<<grid_for(n, 256, (int64_t)ctx->num_sms * refit_per_sm), 256, 0, st>>>(
+      b->pos, b->idx, n, b->d_tri_off, b->d_node_off, b->n_scenes, b->d_perm, b->d_parent, b->d_leaf_parent,
+      b->d_nodes2, b->d_flags, b->d_tris, ctx->spin_limit, ctx->d_err);
   FLG_LAUNCH_CHECK(ctx, "k_refit");
   if (b->width > 2) return collapse_enqueue(ctx, b, b->width, b->leaf_size);
   return FLG_OK;
@@ -573,6 +648,11 @@ FLG_API int flg_bvh_download(flg_bvh bvh, int32_t scene, flg_bvh_topology *t) {
   if (e != cudaSuccess) return cuda_fail(ctx, e, "download");
   if (t->perm)
     for (int64_t i = 0; i < n; ++i) t->perm[i] -= (int32_t)toff;
+  // Device parent links carry the child's side in bit 0.
+  if (t->parent)
+    for (int64_t i = 0; i < m; ++i) t->parent[i] >>= 1;
+  if (t->leaf_parent)
+    for (int64_t i = 0; i < n; ++i) t->leaf_parent[i] >>= 1;
   if (t->leaf_parent && n == 1) t->leaf_parent[0] = -1;  // a lone leaf is the root
   return FLG_OK;
 }

@@ -58,6 +58,10 @@ __device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, co
   }
 }
 
+// One wide node per queued BVH2 node.  The new wide slots and queue entries
+// of a warp are claimed with one atomic per counter (warp prefix sum of the
+// lanes' internal children): per-child atomics on the two shared counters
+// serialised in L2.
 template <int W>
 __global__ void __launch_bounds__(128)
     k_collapse_level(const Node2 *__restrict__ nodes2, const int32_t *__restrict__ range_j,
@@ -65,13 +69,27 @@ __global__ void __launch_bounds__(128)
                      const int2 *__restrict__ q_in, const int32_t *__restrict__ q_in_count, int2 *__restrict__ q_out,
                      int32_t *q_out_count, int32_t *node_ctr, int64_t cap, NodeW<W> *__restrict__ wide,
                      uint32_t *err) {
-  const int cnt = *q_in_count;
-  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < cnt; it += gridDim.x * blockDim.x) {
-    const int2 item = q_in[it];
+  // Counts beyond the queue capacity only arise from a corrupted tree.
+  const int cnt = (int)min((int64_t)*q_in_count, cap);
+  const int lane = threadIdx.x & 31;
+  // Warp-uniform loop: all lanes of a warp share it0.
+  for (int it0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) & ~31u); it0 < cnt;
+       it0 += gridDim.x * blockDim.x) {
+    const int it = it0 + lane;
+    const bool valid = it < cnt;
+    int2 item = make_int2(0, 0);
     Cand c[W];
-    int nc = 2;
-    child_cands(nodes2, range_j, tri_off, node_off, item.x, c[0], c[1]);
-    while (nc < W) {
+    int nc = 0;
+    if (valid) {
+      item = q_in[it];
+      if (item.x < 0 || item.y < 0 || item.x >= cap || item.y >= cap) {
+        atomicOr(err, kErrQueue);  // a hole left by an overflowing level
+      } else {
+        nc = 2;
+        child_cands(nodes2, range_j, tri_off, node_off, item.x, c[0], c[1]);
+      }
+    }
+    while (nc >= 2 && nc < W) {
       int best = -1;
       float ba = -1.0f;
 #pragma unroll
@@ -98,6 +116,26 @@ __global__ void __launch_bounds__(128)
       }
       ++nc;
     }
+    // Children that become wide nodes of the next level.
+    int need = 0;
+#pragma unroll
+    for (int k = 0; k < W; ++k)
+      if (k < nc && c[k].ref >= 0 && c[k].count > leaf_size) ++need;
+    int incl = need;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    int slot0 = 0, q0 = 0;
+    if (lane == 31 && total > 0) {
+      slot0 = atomicAdd(node_ctr, total);
+      q0 = atomicAdd(q_out_count, total);
+    }
+    slot0 = __shfl_sync(0xFFFFFFFFu, slot0, 31) + incl - need;
+    q0 = __shfl_sync(0xFFFFFFFFu, q0, 31) + incl - need;
+    if (!valid || nc == 0) continue;
     NodeW<W> out;
 #pragma unroll
     for (int k = 0; k < W; ++k) {
@@ -111,13 +149,14 @@ __global__ void __launch_bounds__(128)
         if (c[k].ref < 0 || c[k].count <= leaf_size) {
           out.child[k] = ~((c[k].first << 3) | (c[k].count - 1));
         } else {
-          int slot = atomicAdd(node_ctr, 1);
+          const int slot = slot0++;
           if (slot >= cap) {
             atomicOr(err, kErrQueue);
+            if (q0 < cap) q_out[q0] = make_int2(-1, -1);  // the next level skips it
+            ++q0;
             out.child[k] = kEmptyChild;
           } else {
-            int qi = atomicAdd(q_out_count, 1);
-            q_out[qi] = make_int2(c[k].ref, slot);
+            q_out[q0++] = make_int2(c[k].ref, slot);
             out.child[k] = slot;
           }
         }

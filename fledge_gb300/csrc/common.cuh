@@ -172,14 +172,15 @@ __device__ __forceinline__ float3 f3cross(float3 a, float3 b) {
   return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 
-__device__ __forceinline__ bool pluecker(float3 a, float3 b, float3 c, float3 O, float3 D, float &t,
-                                         float &u, float &v) {
+// Hit test and t only; U, V and U+V+W are returned for the barycentrics.
+__device__ __forceinline__ bool pluecker_core(float3 a, float3 b, float3 c, float3 O, float3 D, float &t, float &U,
+                                              float &V, float &UVW) {
   float3 v0 = f3sub(a, O), v1 = f3sub(b, O), v2 = f3sub(c, O);
   float3 e0 = f3sub(v2, v0), e1 = f3sub(v0, v1), e2 = f3sub(v1, v2);
-  float U = f3dot(f3cross(e0, f3add(v2, v0)), D);
-  float V = f3dot(f3cross(e1, f3add(v0, v1)), D);
+  U = f3dot(f3cross(e0, f3add(v2, v0)), D);
+  V = f3dot(f3cross(e1, f3add(v0, v1)), D);
   float W = f3dot(f3cross(e2, f3add(v1, v2)), D);
-  float UVW = U + V + W;
+  UVW = U + V + W;
   float eps = 1.1920928955078125e-07f * fabsf(UVW);
   bool valid = fminf(U, fminf(V, W)) >= -eps || fmaxf(U, fmaxf(V, W)) <= eps;
   if (!valid) return false;
@@ -196,10 +197,23 @@ __device__ __forceinline__ bool pluecker(float3 a, float3 b, float3 c, float3 O,
   if (!(0.0f <= tt)) return false;
   if (!(den != 0.0f)) return false;
   t = tt;
+  return true;
+}
+
+// The traversal's test: t only (the closest hit's barycentrics are formed
+// once, for the winner).
+__device__ __forceinline__ bool pluecker_t(float3 a, float3 b, float3 c, float3 O, float3 D, float &t) {
+  float U, V, UVW;
+  return pluecker_core(a, b, c, O, D, t, U, V, UVW);
+}
+
+__device__ __forceinline__ bool pluecker(float3 a, float3 b, float3 c, float3 O, float3 D, float &t,
+                                         float &u, float &v) {
+  float U, V, UVW;
+  if (!pluecker_core(a, b, c, O, D, t, U, V, UVW)) return false;
   if (UVW != 0.0f) {
-    float r = UVW;
-    u = __fdiv_rn(U, r);
-    v = __fdiv_rn(V, r);
+    u = __fdiv_rn(U, UVW);
+    v = __fdiv_rn(V, UVW);
   } else {
     u = 0.0f;
     v = 0.0f;

@@ -65,20 +65,16 @@ __device__ __forceinline__ int32_t scene_root(const int32_t *__restrict__ roots,
 
 // Tests sorted triangle g; updates the closest hit.  Returns true on accept.
 __device__ __forceinline__ bool test_tri(const TriRec *__restrict__ tris, int64_t g, const float3 &o,
-                                         const float3 &d, float tmin, float &best, bool &have, int32_t &prim,
-                                         float &hu, float &hv) {
+                                         const float3 &d, float tmin, float &best, bool &have, int32_t &prim) {
   const float4 *p = (const float4 *)(tris + g);
   float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
-  float t, u, v;
-  if (!pluecker(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z), o, d, t,
-                u, v))
+  float t;
+  if (!pluecker_t(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z), o, d, t))
     return false;
   if (!accept_closest(t, tmin, best, have)) return false;
   best = t;
   have = true;
   prim = (int32_t)g;  // sorted position; write_result maps it to the original id
-  hu = u;
-  hv = v;
   return true;
 }
 
@@ -87,9 +83,8 @@ __device__ __forceinline__ bool test_tri_any(const TriRec *__restrict__ tris, in
                                              const float3 &d, float tmin, float tmax) {
   const float4 *p = (const float4 *)(tris + g);
   float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
-  float t, u, v;
-  if (!pluecker(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z), o, d, t,
-                u, v))
+  float t;
+  if (!pluecker_t(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z), o, d, t))
     return false;
   return t >= tmin && !(t > tmax);
 }
@@ -100,18 +95,23 @@ __device__ __forceinline__ uint64_t stack_key(float t, int32_t ref) {
 
 // Writes one ray's result.  For closest hit, `prim` holds the sorted
 // position of the winning triangle: its record gives the original id and the
-// vertices for the double-precision refinement of t, u, v.
+// vertices for the float-float refinement of t, u, v.  The traversal keeps
+// only t; the fp32 barycentrics (pluecker) are formed here, for the winner,
+// and replaced by the refined ones unless the refinement finds den == 0.
 __device__ __forceinline__ void write_result(const Out &O, int64_t i, bool any, bool have, int32_t prim,
-                                             float best, float tmax, float u, float v,
-                                             const TriRec *__restrict__ tris, const float3 &o, const float3 &d) {
+                                             float best, float tmax, const TriRec *__restrict__ tris,
+                                             const float3 &o, const float3 &d) {
+  float u = 0.0f, v = 0.0f;
   if (any) {
     O.occ[i] = have ? 1 : 0;
   } else {
     if (have) {
       const float4 *p = (const float4 *)(tris + prim);
       const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
-      refine_tuv(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z), o, d, best,
-                 u, v);
+      const float3 pa = make_float3(a.x, a.y, a.z), pb = make_float3(b.x, b.y, b.z), pc = make_float3(c.x, c.y, c.z);
+      float tf;
+      pluecker(pa, pb, pc, o, d, tf, u, v);
+      refine_tuv(pa, pb, pc, o, d, best, u, v);
       prim = __float_as_int(a.w);
     }
     O.prim[i] = have ? prim : -1;
@@ -133,16 +133,14 @@ __device__ __forceinline__ void record_overflow(const Scratch &S, int64_t ray) {
 template <bool ANY, int STACK>
 __device__ __forceinline__ bool trace_bvh2(const Node2 *__restrict__ nodes, const TriRec *__restrict__ tris,
                                            int32_t root, const float3 &o, const float3 &d, const float3 &inv,
-                                           float tmin, float tmax, bool &have, int32_t &prim, float &best,
-                                           float &hu, float &hv) {
+                                           float tmin, float tmax, bool &have, int32_t &prim, float &best) {
   best = tmax;
   have = false;
   prim = -1;
-  hu = hv = 0.0f;
   if (root == INT32_MIN) return true;
   if (root < 0) {
     if (ANY) have = test_tri_any(tris, ~(int64_t)root, o, d, tmin, tmax);
-    else test_tri(tris, ~(int64_t)root, o, d, tmin, best, have, prim, hu, hv);
+    else test_tri(tris, ~(int64_t)root, o, d, tmin, best, have, prim);
     return true;
   }
   uint64_t stk[STACK];
@@ -158,14 +156,14 @@ __device__ __forceinline__ bool trace_bvh2(const Node2 *__restrict__ nodes, cons
       if (ANY) {
         if (test_tri_any(tris, ~(int64_t)c0, o, d, tmin, tmax)) { have = true; return true; }
       } else {
-        test_tri(tris, ~(int64_t)c0, o, d, tmin, best, have, prim, hu, hv);
+        test_tri(tris, ~(int64_t)c0, o, d, tmin, best, have, prim);
       }
     }
     if (c1 < 0) {
       if (ANY) {
         if (test_tri_any(tris, ~(int64_t)c1, o, d, tmin, tmax)) { have = true; return true; }
       } else {
-        test_tri(tris, ~(int64_t)c1, o, d, tmin, best, have, prim, hu, hv);
+        test_tri(tris, ~(int64_t)c1, o, d, tmin, best, have, prim);
       }
     }
     const float lim = ANY ? tmax : best;
@@ -205,60 +203,105 @@ __global__ void __launch_bounds__(256)
   const int32_t root = scene_root(roots, ray_off, n_scenes, i);
   bool have;
   int32_t prim;
-  float best, hu, hv;
-  if (!trace_bvh2<ANY, 64>(nodes, tris, root, o, d, inv, tmin, tmax, have, prim, best, hu, hv)) {
+  float best;
+  if (!trace_bvh2<ANY, 64>(nodes, tris, root, o, d, inv, tmin, tmax, have, prim, best)) {
     record_overflow(S, i);
     return;
   }
-  write_result(O, i, ANY, have, prim, best, tmax, hu, hv, tris, o, d);
+  write_result(O, i, ANY, have, prim, best, tmax, tris, o, d);
 }
 
 // ----------------------------------------------------------------------------
 // Wide traversal as a resumable state machine (one node or leaf range per
 // step) so the persistent kernel can swap rays between steps.
 // ----------------------------------------------------------------------------
-template <int W>
-__device__ __forceinline__ void cas(uint64_t &a, uint64_t &b) {
-  uint64_t lo = a < b ? a : b, hi = a < b ? b : a;
+// Child keys for the nearest-first order: the bits of tnear (non-negative,
+// so integer order is float order) with the child's slot in the low
+// log2(W) bits.  Dropping those mantissa bits only rounds tnear down, which
+// keeps the stack's culling test (entry tnear > best) conservative.
+__device__ __forceinline__ void cas(uint32_t &a, uint32_t &b) {
+  const uint32_t lo = min(a, b), hi = max(a, b);
   a = lo;
   b = hi;
 }
 
 template <int W>
-__device__ __forceinline__ void sort_keys(uint64_t (&k)[W]) {
+__device__ __forceinline__ void sort_keys(uint32_t (&k)[W]) {
   if constexpr (W == 4) {
-    cas<W>(k[0], k[1]); cas<W>(k[2], k[3]); cas<W>(k[0], k[2]); cas<W>(k[1], k[3]); cas<W>(k[1], k[2]);
+    cas(k[0], k[1]); cas(k[2], k[3]); cas(k[0], k[2]); cas(k[1], k[3]); cas(k[1], k[2]);
   } else {
-    cas<W>(k[0], k[1]); cas<W>(k[2], k[3]); cas<W>(k[4], k[5]); cas<W>(k[6], k[7]);
-    cas<W>(k[0], k[2]); cas<W>(k[1], k[3]); cas<W>(k[4], k[6]); cas<W>(k[5], k[7]);
-    cas<W>(k[1], k[2]); cas<W>(k[5], k[6]);
-    cas<W>(k[0], k[4]); cas<W>(k[1], k[5]); cas<W>(k[2], k[6]); cas<W>(k[3], k[7]);
-    cas<W>(k[2], k[4]); cas<W>(k[3], k[5]);
-    cas<W>(k[1], k[2]); cas<W>(k[3], k[4]); cas<W>(k[5], k[6]);
+    cas(k[0], k[1]); cas(k[2], k[3]); cas(k[4], k[5]); cas(k[6], k[7]);
+    cas(k[0], k[2]); cas(k[1], k[3]); cas(k[4], k[6]); cas(k[5], k[7]);
+    cas(k[1], k[2]); cas(k[5], k[6]);
+    cas(k[0], k[4]); cas(k[1], k[5]); cas(k[2], k[6]); cas(k[3], k[7]);
+    cas(k[2], k[4]); cas(k[3], k[5]);
+    cas(k[1], k[2]); cas(k[3], k[4]); cas(k[5], k[6]);
   }
 }
 
+// The child ref a sorted key names (selects, no dynamic register index).
+template <int W>
+__device__ __forceinline__ int32_t key_ref(uint32_t key, const int32_t (&ref)[W]) {
+  const uint32_t slot = key & (uint32_t)(W - 1);
+  int32_t r = ref[0];
+#pragma unroll
+  for (int m = 1; m < W; ++m) r = slot == (uint32_t)m ? ref[m] : r;
+  return r;
+}
+
+// Stack entry (tnear rounded down | ref) of a sorted key.
+template <int W>
+__device__ __forceinline__ uint64_t key_entry(uint32_t key, const int32_t (&ref)[W]) {
+  return ((uint64_t)(key & ~(uint32_t)(W - 1)) << 32) | (uint32_t)key_ref<W>(key, ref);
+}
+
 // Tests the W children of a wide node (7 / 14 16-byte loads) with the
-// reference's slab test (slab_tnear).  Returns the number of children hit
-// with tnear <= lim; their keys (tnear | ref) are in key[], misses are ~0.
+// reference's slab test (BoundIntersect, intersector.hpp:103-120).  The
+// near and far plane arrays of each axis are picked by the sign of the
+// ray's inverse direction when they are loaded, so the per-child swap of
+// slab1 disappears; the products are the same roundings, so tnear and the
+// hit decision equal slab_tnear's (a NaN slab, 0 * inf, constrains nothing
+// in both).  Returns the number of children hit with tnear <= lim; their
+// keys are in key[] (misses are ~0), the child refs in ref[].
 template <int W>
 __device__ __forceinline__ int visit_node(const NodeW<W> *__restrict__ node, const float3 &o, const float3 &inv,
-                                          float lim, uint64_t (&key)[W]) {
-  constexpr int NV = 7 * W / 4;
-  float f[4 * NV];
+                                          float lim, uint32_t (&key)[W], int32_t (&ref)[W]) {
+  constexpr int Q = W / 4;  // float4s per child array
   const float4 *np = (const float4 *)node;
+  // Float4 offsets of the near arrays: lo (sign 0) or hi (sign 1) per axis.
+  const int nx = (int)(__float_as_uint(inv.x) >> 31) * Q;
+  const int ny = 2 * Q + (int)(__float_as_uint(inv.y) >> 31) * Q;
+  const int nz = 4 * Q + (int)(__float_as_uint(inv.z) >> 31) * Q;
+  float pn[3][W], pf[3][W];
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    const float4 q = __ldg(np + k);
-    f[4 * k] = q.x; f[4 * k + 1] = q.y; f[4 * k + 2] = q.z; f[4 * k + 3] = q.w;
+  for (int h = 0; h < Q; ++h) {
+    const float4 a = __ldg(np + nx + h), b = __ldg(np + (nx ^ Q) + h);
+    const float4 c = __ldg(np + ny + h), e = __ldg(np + (ny ^ Q) + h);
+    const float4 f = __ldg(np + nz + h), g = __ldg(np + (nz ^ Q) + h);
+    const int4 r = __ldg((const int4 *)np + 6 * Q + h);
+    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+    const float cv[4] = {c.x, c.y, c.z, c.w}, ev[4] = {e.x, e.y, e.z, e.w};
+    const float fv[4] = {f.x, f.y, f.z, f.w}, gv[4] = {g.x, g.y, g.z, g.w};
+    const int32_t rv[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      pn[0][4 * h + k] = av[k]; pf[0][4 * h + k] = bv[k];
+      pn[1][4 * h + k] = cv[k]; pf[1][4 * h + k] = ev[k];
+      pn[2][4 * h + k] = fv[k]; pf[2][4 * h + k] = gv[k];
+      ref[4 * h + k] = rv[k];
+    }
   }
+  const float t1c = fminf(lim, 3.402823466e+38f);
   int nh = 0;
 #pragma unroll
   for (int k = 0; k < W; ++k) {
-    const int32_t ref = __float_as_int(f[6 * W + k]);
-    const float t = slab_tnear(f[k], f[W + k], f[2 * W + k], f[3 * W + k], f[4 * W + k], f[5 * W + k], o, inv);
-    const bool ok = ref != kEmptyChild && t <= lim;
-    key[k] = ok ? stack_key(t, ref) : ~0ull;
+    const float tnx = (pn[0][k] - o.x) * inv.x, tfx = (pf[0][k] - o.x) * inv.x;
+    const float tny = (pn[1][k] - o.y) * inv.y, tfy = (pf[1][k] - o.y) * inv.y;
+    const float tnz = (pn[2][k] - o.z) * inv.z, tfz = (pf[2][k] - o.z) * inv.z;
+    const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+    const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, t1c));
+    const bool ok = ref[k] != kEmptyChild && t0 <= t1;
+    key[k] = ok ? ((__float_as_uint(t0) & 0x7FFFFFFFu & ~(uint32_t)(W - 1)) | (uint32_t)k) : ~0u;
     nh += ok ? 1 : 0;
   }
   return nh;
@@ -267,7 +310,7 @@ __device__ __forceinline__ int visit_node(const NodeW<W> *__restrict__ node, con
 template <int W, bool ANY, int STACK>
 struct Tracer {
   float3 o, d, inv;
-  float tmin, tmax, best, hu, hv;
+  float tmin, tmax, best;
   int32_t cur, prim;
   int sp;
   bool have, overflow;
@@ -278,7 +321,6 @@ struct Tracer {
     have = false;
     overflow = false;
     prim = -1;
-    hu = hv = 0.0f;
     sp = 0;
     cur = root;
   }
@@ -298,8 +340,9 @@ struct Tracer {
   __device__ __forceinline__ bool step(const NodeW<W> *__restrict__ nodes, const TriRec *__restrict__ tris) {
     if (cur == kEmptyChild || cur == INT32_MIN) return true;
     if (cur >= 0) {
-      uint64_t key[W];
-      const int nh = visit_node<W>(nodes + cur, o, inv, ANY ? tmax : best, key);
+      uint32_t key[W];
+      int32_t ref[W];
+      const int nh = visit_node<W>(nodes + cur, o, inv, ANY ? tmax : best, key, ref);
       if (nh == 0) return !pop();
       sort_keys<W>(key);
       if (sp + nh - 1 > STACK) {
@@ -308,8 +351,8 @@ struct Tracer {
       }
 #pragma unroll
       for (int k = W - 1; k >= 1; --k)
-        if (k < nh) stk[sp++] = key[k];
-      cur = (int32_t)(uint32_t)key[0];
+        if (k < nh) stk[sp++] = key_entry<W>(key[k], ref);
+      cur = key_ref<W>(key[0], ref);
       return false;
     }
     const int32_t enc = ~cur;
@@ -322,7 +365,7 @@ struct Tracer {
           return true;
         }
       } else {
-        test_tri(tris, first + j, o, d, tmin, best, have, prim, hu, hv);
+        test_tri(tris, first + j, o, d, tmin, best, have, prim);
       }
     }
     return !pop();
@@ -341,7 +384,7 @@ __global__ void __launch_bounds__(256)
   while (!tr.step(nodes, tris)) {
   }
   if (tr.overflow) record_overflow(S, i);
-  else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv, tris, tr.o, tr.d);
+  else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tris, tr.o, tr.d);
 }
 
 template <int W, bool ANY, int STACK>
@@ -378,7 +421,7 @@ __global__ void __launch_bounds__(256)
     }
     if (active && tr.step(nodes, tris)) {
       if (tr.overflow) record_overflow(S, ray);
-      else write_result(O, ray, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv, tris, tr.o, tr.d);
+      else write_result(O, ray, ANY, tr.have, tr.prim, tr.best, tr.tmax, tris, tr.o, tr.d);
       active = false;
     }
   }
@@ -400,12 +443,12 @@ __global__ void __launch_bounds__(128)
     if (W == 2) {
       bool have;
       int32_t prim;
-      float best, hu, hv;
-      if (!trace_bvh2<ANY, kRetryStack>(nodes2, tris, root, o, d, inv, tmin, tmax, have, prim, best, hu, hv)) {
+      float best;
+      if (!trace_bvh2<ANY, kRetryStack>(nodes2, tris, root, o, d, inv, tmin, tmax, have, prim, best)) {
         atomicOr(S.err, kErrStack);
         continue;
       }
-      write_result(O, i, ANY, have, prim, best, tmax, hu, hv, tris, o, d);
+      write_result(O, i, ANY, have, prim, best, tmax, tris, o, d);
     } else {
       Tracer<(W == 2 ? 4 : W), ANY, kRetryStack> tr;
       tr.o = o; tr.d = d; tr.inv = inv; tr.tmin = tmin; tr.tmax = tmax;
@@ -413,7 +456,7 @@ __global__ void __launch_bounds__(128)
       while (!tr.step(nodes, tris)) {
       }
       if (tr.overflow) atomicOr(S.err, kErrStack);
-      else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tr.hu, tr.hv, tris, tr.o, tr.d);
+      else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tris, tr.o, tr.d);
     }
   }
 }
@@ -464,7 +507,7 @@ __global__ void __launch_bounds__(256, 4)
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt = (1u << lane) - 1u;
   float3 o = make_float3(0.f, 0.f, 0.f), d = o, inv = o;
-  float tmin = 0.f, tmax = 0.f, best = 0.f, hu = 0.f, hv = 0.f;
+  float tmin = 0.f, tmax = 0.f, best = 0.f;
   int32_t prim = -1, cur = kNone, leaf = kNone;
   int sp = 0;
   bool have = false, active = false, overflow = false, exhausted = false;
@@ -485,7 +528,7 @@ __global__ void __launch_bounds__(256, 4)
     // Retire finished rays.
     if (active && cur == kNone && leaf == kNone) {
       if (overflow) record_overflow(S, ray);
-      else write_result(O, ray, ANY, have, prim, best, tmax, hu, hv, tris, o, d);
+      else write_result(O, ray, ANY, have, prim, best, tmax, tris, o, d);
       active = false;
     }
     // Refill idle lanes.
@@ -504,8 +547,7 @@ __global__ void __launch_bounds__(256, 4)
           have = false;
           overflow = false;
           prim = -1;
-          hu = hv = 0.0f;
-          sp = 0;
+                sp = 0;
           leaf = kNone;
           cur = scene_root(roots, ray_off, n_scenes, ray);
           if (cur == INT32_MIN) cur = kNone;
@@ -528,8 +570,9 @@ __global__ void __launch_bounds__(256, 4)
       const bool at_node = active && cur >= 0 && cur != kNone;
       if (!__any_sync(0xFFFFFFFFu, at_node)) break;
       if (at_node) {
-        uint64_t key[W];
-        const int nh = visit_node<W>(nodes + cur, o, inv, ANY ? tmax : best, key);
+        uint32_t key[W];
+        int32_t ref[W];
+        const int nh = visit_node<W>(nodes + cur, o, inv, ANY ? tmax : best, key, ref);
         if (nh == 0) {
           cur = pop();
         } else {
@@ -541,8 +584,8 @@ __global__ void __launch_bounds__(256, 4)
           } else {
 #pragma unroll
             for (int k = W - 1; k >= 1; --k)
-              if (k < nh) stk[sp++] = key[k];
-            cur = (int32_t)(uint32_t)key[0];
+              if (k < nh) stk[sp++] = key_entry<W>(key[k], ref);
+            cur = key_ref<W>(key[0], ref);
           }
         }
       }
@@ -564,7 +607,7 @@ __global__ void __launch_bounds__(256, 4)
             break;
           }
         } else {
-          test_tri(tris, first + j, o, d, tmin, best, have, prim, hu, hv);
+          test_tri(tris, first + j, o, d, tmin, best, have, prim);
         }
       }
       leaf = kNone;
