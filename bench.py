@@ -38,10 +38,10 @@ N_SCENES = 256
 RAYS_PER_TRI = 64
 SEED_C0, SEED_C2, SEED_C3 = 0xF1ED0000, 0xF1ED0002, 0xF1ED0003
 # Algorithmic bytes (compulsory DRAM traffic): per ray 6 floats in + prim, t,
-# u, v out; per triangle of a batched build: bounds 36 + Morton 44 + sort
-# (histogram 4 + 5 passes x 24 counting the scene pass) + Karras 20 + refit 100.
+# u, v out; per triangle of a batched build: bounds 36 + Morton 44 + sort of
+# (scene, code) keys (histogram 8 + 5 passes x 24) + Karras 20 + refit 100.
 BYTES_PER_RAY = 24 + 16
-BYTES_PER_TRI_BATCHED = 36 + 44 + (4 + 5 * 24) + 20 + 100
+BYTES_PER_TRI_BATCHED = 36 + 44 + (8 + 5 * 24) + 20 + 100
 
 
 _T0 = time.perf_counter()

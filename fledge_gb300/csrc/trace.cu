@@ -242,11 +242,17 @@ __device__ __forceinline__ void sort_keys(uint32_t (&k)[W]) {
 // The child ref a sorted key names (selects, no dynamic register index).
 template <int W>
 __device__ __forceinline__ int32_t key_ref(uint32_t key, const int32_t (&ref)[W]) {
-  const uint32_t slot = key & (uint32_t)(W - 1);
-  int32_t r = ref[0];
+  if constexpr (W == 4) {
+    const int32_t a = (key & 1u) ? ref[1] : ref[0];
+    const int32_t b = (key & 1u) ? ref[3] : ref[2];
+    return (key & 2u) ? b : a;
+  } else {
+    const uint32_t slot = key & (uint32_t)(W - 1);
+    int32_t r = ref[0];
 #pragma unroll
-  for (int m = 1; m < W; ++m) r = slot == (uint32_t)m ? ref[m] : r;
-  return r;
+    for (int m = 1; m < W; ++m) r = slot == (uint32_t)m ? ref[m] : r;
+    return r;
+  }
 }
 
 // Stack entry (tnear rounded down | ref) of a sorted key.
@@ -547,7 +553,7 @@ __global__ void __launch_bounds__(256, 4)
           have = false;
           overflow = false;
           prim = -1;
-                sp = 0;
+          sp = 0;
           leaf = kNone;
           cur = scene_root(roots, ray_off, n_scenes, ray);
           if (cur == INT32_MIN) cur = kNone;
