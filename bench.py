@@ -337,6 +337,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     c4 = run_c4(ctx, torch, F, dev, pk) if not args.skip_c4 else None
     log("config 1")
     c1 = run_c1(ctx, torch, F, dev, rank == 0 and not args.skip_cpu) if not args.skip_c1 else None
+    log("config 1 with a medium")
+    c1v = run_c1_volume(ctx, torch, F, dev, rank == 0 and not args.skip_cpu) if not args.skip_c1 else None
 
     # ---- CPU baseline (rank 0) ----
     log('volume done')
@@ -366,7 +368,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                            "parallelism": f"replicas x{world}"},
                 "build_ms": round(b_ms, 3), "trace_ms": round(tr_ms, 3), "hit_rate": round(hit_rate, 4),
                 "build_roofline": build_roof, "roofline": roof, "plain": plain, "volume": vol,
-                "config0": c0, "config1": c1, "config4": c4,
+                "config0": c0, "config1": c1, "config1_volume": c1v, "config4": c4,
                 "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches),
                 "gpu_launches_total": int(total_launches)}
         print(json.dumps(line), flush=True)
@@ -544,6 +546,50 @@ def run_c1(ctx, torch, F, dev, with_cpu: bool):
         t0 = time.perf_counter()
         _, rays = O.pathtrace(pos, ind, tree, lfirst, 2, (10, 10, 10), (0.7, 0.7, 0.7), C1_CAMERA["eye"],
                               C1_CAMERA["target"], C1_CAMERA["up"], C1_CAMERA["fov_deg"], 1920, 1080, 16, 5, stride)
+        cdt = time.perf_counter() - t0
+        res["cpu_mrays_s"] = round(sum(rays) / cdt / 1e6, 3)
+        res["cpu_sample"] = f"every {stride}th pixel ({sum(rays)} rays, {cdt:.1f} s, {os.cpu_count()} threads)"
+    b.destroy()
+    return res
+
+
+def run_c1_volume(ctx, torch, F, dev, with_cpu: bool):
+    """Volumetric path tracing (VolPathIntegrator::Li) of the config-1 scene
+    with a 128^3 noise medium (densities in [0, 0.8], sigma_s 0.8, sigma_a 0.2,
+    g 0.3) filling the box [-1.5, 1.5]^3 around the sphere: 1920x1080 at
+    4 spp, depth 5.  Mrays/s over closest-hit and shadow rays (the free-flight
+    and ratio-tracking steps are extra work per ray)."""
+    pos, ind, lfirst = c1_scene()
+    p, i = torch.from_numpy(pos).to(dev), torch.from_numpy(ind).to(dev)
+    b = F.RadixBVHBuilder(F.InternalTriangleMesh(p, i), ctx, node_width=4, leaf_size=2)
+    b.build()
+    rho = F.gen_noise_grid(ctx, 128, SEED_C2 + 16, scale=0.8)
+    lo, hi = (-1.5, -1.5, -1.5), (1.5, 1.5, 1.5)
+    vol = F.DenseGridVolume(rho, lo, hi, F.Medium(0.8, 0.2, 0.3), ctx)
+    seed = SEED_C2 + 17
+    F.pathtrace(ctx, b, lfirst, 2, width=1920, height=1080, spp=1, max_depth=5, volume=vol, seed=seed,
+                **C1_CAMERA)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    img, stats = F.pathtrace(ctx, b, lfirst, 2, width=1920, height=1080, spp=4, max_depth=5, volume=vol, seed=seed,
+                             **C1_CAMERA)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    n = stats["closest_rays"] + stats["shadow_rays"]
+    res = {"workload": "config 1 + 128^3 medium around the sphere, 1920x1080x4 spp, depth 5",
+           "ms": round(dt * 1e3, 2), "mrays_s": round(n / dt / 1e6, 1), "closest_rays": stats["closest_rays"],
+           "shadow_rays": stats["shadow_rays"], "mean_radiance": round(float(img.mean()), 6)}
+    if with_cpu:
+        from oracle import oracle as O
+        O.build()
+        O.set_threads(os.cpu_count() or 1)
+        tree = O.build_bvh(pos, ind)
+        stride = 23
+        grid = (rho.cpu().numpy(), lo, hi, O.Medium(0.8, 0.2, 0.3, 0.1, 0.0))
+        t0 = time.perf_counter()
+        _, rays = O.pathtrace(pos, ind, tree, lfirst, 2, (10, 10, 10), (0.7, 0.7, 0.7), C1_CAMERA["eye"],
+                              C1_CAMERA["target"], C1_CAMERA["up"], C1_CAMERA["fov_deg"], 1920, 1080, 4, 5, stride,
+                              grid=grid, seed=seed)
         cdt = time.perf_counter() - t0
         res["cpu_mrays_s"] = round(sum(rays) / cdt / 1e6, 3)
         res["cpu_sample"] = f"every {stride}th pixel ({sum(rays)} rays, {cdt:.1f} s, {os.cpu_count()} threads)"

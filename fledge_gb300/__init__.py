@@ -30,7 +30,7 @@ from ._lib import (FlgBuildOpts, FlgBvhInfo, FlgBvhTopology, FlgError, FlgHits, 
                    FlgTraceOpts, FlgTrCkpt, check, load)
 
 __all__ = ["Context", "InternalTriangleMesh", "RadixBVHBuilder", "BatchedRadixBVHBuilder", "Rays",
-           "DenseGridVolume", "Medium", "hit_adjoint", "gen_triangles", "gen_rays", "gen_noise_grid",
+           "DenseGridVolume", "SparseGridVolume", "Medium", "hit_adjoint", "gen_triangles", "gen_rays", "gen_noise_grid", "read_ply",
            "FlgError", "load"]
 
 
@@ -348,6 +348,66 @@ class DenseGridVolume:
             pass
 
 
+class SparseGridVolume(DenseGridVolume):
+    """The same medium on a sparse grid of 8^3 bricks (the NanoVDBVolume that
+    volume.hpp:72-92 declares): ``from_dense`` keeps the bricks with a
+    non-zero voxel.  ``density`` is the [n_bricks, 8, 8, 8] brick array;
+    ``tr_adjoint`` gradients have that shape."""
+
+    BRICK = 8
+
+    def __init__(self, brick_index, bricks, shape, box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0),
+                 medium: Medium = Medium(), ctx: Optional[Context] = None):
+        self.ctx = ctx or Context(brick_index.device.index or 0)
+        self.brick_index = brick_index  # [bnz, bny, bnx] int32, slot or -1
+        self.density = bricks           # [n_bricks, 8, 8, 8] float32
+        self.shape = tuple(shape)       # (nz, ny, nx) of the lattice
+        nz, ny, nx = self.shape
+        lo = (C.c_float * 3)(*box_lo)
+        hi = (C.c_float * 3)(*box_hi)
+        m = medium.struct()
+        h = C.c_void_p()
+        self.ctx.check(self.ctx.lib.flg_grid_create_sparse(
+            self.ctx.h, C.c_void_p(_ptr(brick_index)), C.c_void_p(_ptr(bricks) if bricks.numel() else None),
+            int(bricks.shape[0]), nx, ny, nz, lo, hi, C.byref(m), C.byref(h)))
+        self.h = h
+        self.medium = medium
+
+    @classmethod
+    def from_dense(cls, density, box_lo=(0.0, 0.0, 0.0), box_hi=(1.0, 1.0, 1.0), medium: Medium = Medium(),
+                   ctx: Optional[Context] = None) -> "SparseGridVolume":
+        torch = _torch()
+        ctx = ctx or Context(density.device.index or 0)
+        nz, ny, nx = density.shape
+        b = cls.BRICK
+        bidx = torch.empty(((nz + b - 1) // b, (ny + b - 1) // b, (nx + b - 1) // b), dtype=torch.int32,
+                           device=density.device)
+        cnt = C.c_int64()
+        lib = ctx.lib
+        ctx.check(lib.flg_grid_sparsify(ctx.h, C.c_void_p(_ptr(density)), nx, ny, nz, C.c_void_p(_ptr(bidx)), None,
+                                        0, C.byref(cnt)))
+        bricks = torch.empty((cnt.value, b, b, b), dtype=torch.float32, device=density.device)
+        if cnt.value:
+            ctx.check(lib.flg_grid_sparsify(ctx.h, C.c_void_p(_ptr(density)), nx, ny, nz, C.c_void_p(_ptr(bidx)),
+                                            C.c_void_p(_ptr(bricks)), cnt.value, C.byref(cnt)))
+        return cls(bidx, bricks, (nz, ny, nx), box_lo, box_hi, medium, ctx)
+
+    def to_dense(self, values=None):
+        """Scatters brick-layout values (the densities, or an adjoint
+        gradient) back to the dense [nz, ny, nx] lattice (zeros elsewhere)."""
+        torch = _torch()
+        vals = self.density if values is None else values
+        nz, ny, nx = self.shape
+        b = self.BRICK
+        bz, by, bx = self.brick_index.shape
+        out = torch.zeros((bz * b, by * b, bx * b), dtype=vals.dtype, device=vals.device)
+        full = torch.zeros((bz, by, bx, b, b, b), dtype=vals.dtype, device=vals.device)
+        occ = self.brick_index >= 0
+        full[occ] = vals.reshape(-1, b, b, b)[self.brick_index[occ].long()]
+        out = full.permute(0, 3, 1, 4, 2, 5).reshape(bz * b, by * b, bx * b)
+        return out[:nz, :ny, :nx].contiguous()
+
+
 def hit_adjoint(ctx: Context, mesh: InternalTriangleMesh, rays: Rays, hits, dLdt=None, dLdu=None, dLdv=None,
                 grad=None):
     """dL/dpos for fixed hits (fp32 atomics into a [nVert, 3] tensor)."""
@@ -364,9 +424,11 @@ def hit_adjoint(ctx: Context, mesh: InternalTriangleMesh, rays: Rays, hits, dLdt
 def pathtrace(ctx: Context, bvh: RadixBVHBuilder, light_first: int, light_count: int, light_le=(10.0, 10.0, 10.0),
               albedo=(0.7, 0.7, 0.7), eye=(0.0, 0.5, 4.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0),
               fov_deg: float = 40.0, width: int = 1920, height: int = 1080, spp: int = 16, max_depth: int = 5,
-              **opts):
+              volume: Optional["DenseGridVolume"] = None, seed: int = 0, **opts):
     """Wavefront path tracing of the mesh of `bvh` (PathIntegrator::Li with
-    next-event estimation).  Returns (radiance [height, width, 3], stats)."""
+    next-event estimation; with `volume`, VolPathIntegrator::Li with the
+    grid's medium filling its box).  Returns (radiance [height, width, 3],
+    stats)."""
     torch = _torch()
     mesh = bvh.mesh
     sc = _lib.FlgPtScene(_ptr(mesh.p), _ptr(mesh.ind), mesh.n_tri, mesh.n_vert, light_first, light_count,
@@ -376,9 +438,39 @@ def pathtrace(ctx: Context, bvh: RadixBVHBuilder, light_first: int, light_count:
     out = torch.empty((height, width, 3), dtype=torch.float32, device=mesh.p.device)
     st = _lib.FlgPtStats()
     op = _trace_opts(**opts)
-    ctx.check(ctx.lib.flg_pathtrace(ctx.h, bvh.h, C.byref(sc), C.byref(cam), spp, max_depth, C.byref(op),
-                                    C.c_void_p(_ptr(out)), C.byref(st)))
+    if volume is None:
+        ctx.check(ctx.lib.flg_pathtrace(ctx.h, bvh.h, C.byref(sc), C.byref(cam), spp, max_depth, C.byref(op),
+                                        C.c_void_p(_ptr(out)), C.byref(st)))
+    else:
+        ctx.check(ctx.lib.flg_volpath(ctx.h, bvh.h, volume.h, seed, C.byref(sc), C.byref(cam), spp, max_depth,
+                                      C.byref(op), C.c_void_p(_ptr(out)), C.byref(st)))
     return out, {"closest_rays": st.closest_rays, "shadow_rays": st.shadow_rays}
+
+
+# ------------------------------ mesh ingestion -------------------------------
+
+def read_ply(path: str) -> dict:
+    """Reads a PLY triangle mesh (MakeTriangleMesh, plymesh.cpp:19-86) on the
+    host: dict of pos [n_vert, 3] float32, idx [n_tri, 3] int32, and normal
+    [n_vert, 3] / uv [n_vert, 2] float32 or None."""
+    lib = load()
+    m = _lib.FlgHostMesh()
+    err = C.create_string_buffer(256)
+    code = lib.flg_ply_read(path.encode(), C.byref(m), err, 256)
+    if code != _lib.FLG_OK:
+        raise FlgError(code, err.value.decode() or lib.flg_status_string(code).decode())
+    try:
+        nv, nt = int(m.n_vert), int(m.n_tri)
+
+        def arr(ptr, n, dt, cols):
+            if not ptr or n == 0:
+                return None if not ptr else np.zeros((0, cols), dt)
+            return np.ctypeslib.as_array(ptr, shape=(n * cols,)).astype(dt, copy=True).reshape(n, cols)
+
+        return {"pos": arr(m.pos, nv, np.float32, 3), "idx": arr(m.idx, nt, np.int32, 3),
+                "normal": arr(m.normal, nv, np.float32, 3), "uv": arr(m.uv, nv, np.float32, 2)}
+    finally:
+        lib.flg_host_mesh_free(C.byref(m))
 
 
 # --------------------------- synthetic workloads -----------------------------

@@ -19,8 +19,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libflg.so")
 
 SOURCES = ["api.cu", "build.cu", "sort.cu", "collapse.cu", "trace.cu", "volume.cu",
-           "adjoint.cu", "gen.cu", "pathtrace.cu"]
-HEADERS = [os.path.join(CSRC, "common.cuh"), os.path.join(CSRC, "internal.h"),
+           "adjoint.cu", "gen.cu", "pathtrace.cu", "ply.cpp"]
+HEADERS = [os.path.join(CSRC, "common.cuh"), os.path.join(CSRC, "internal.h"), os.path.join(CSRC, "volume.cuh"),
            os.path.join(ROOT, "include", "flg.h")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -49,7 +49,7 @@ def _stale(obj: str, src: str) -> bool:
 
 def _compile(src: str, verbose: bool) -> str:
     s = os.path.join(CSRC, src)
-    o = os.path.join(OUT, src.replace(".cu", ".o"))
+    o = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
     if _stale(o, s):
         cmd = [nvcc()] + NVCC_FLAGS + ["-c", s, "-o", o]
         if verbose:

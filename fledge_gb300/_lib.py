@@ -55,6 +55,11 @@ class FlgTrCkpt(C.Structure):
     _fields_ = [("t", C.c_void_p), ("k", C.c_void_p), ("c", C.c_void_p)]
 
 
+class FlgHostMesh(C.Structure):
+    _fields_ = [("pos", C.POINTER(C.c_float)), ("normal", C.POINTER(C.c_float)), ("uv", C.POINTER(C.c_float)),
+                ("idx", C.POINTER(C.c_int32)), ("n_vert", C.c_int64), ("n_tri", C.c_int64)]
+
+
 class FlgPtScene(C.Structure):
     _fields_ = [("pos", C.c_void_p), ("idx", C.c_void_p), ("n_tri", C.c_int64), ("n_vert", C.c_int64),
                 ("light_first", C.c_int32), ("light_count", C.c_int32), ("light_le", C.c_float * 3),
@@ -109,6 +114,8 @@ SIGNATURES = {
     "flg_volume_sample": [P, P, C.POINTER(FlgRays), I64, U64, P, P, P],
     "flg_pathtrace": [P, P, C.POINTER(FlgPtScene), C.POINTER(FlgPtCamera), I32, I32, C.POINTER(FlgTraceOpts), P,
                       C.POINTER(FlgPtStats)],
+    "flg_volpath": [P, P, P, C.c_uint64, C.POINTER(FlgPtScene), C.POINTER(FlgPtCamera), I32, I32,
+                    C.POINTER(FlgTraceOpts), P, C.POINTER(FlgPtStats)],
     "flg_graph_begin": [P],
     "flg_graph_end": [P, PP],
     "flg_graph_launch": [P, P],
@@ -117,9 +124,13 @@ SIGNATURES = {
     "flg_gen_rays": [P, U64, I64, I64, C.POINTER(F32), F32, P, P, P, P, P, P],
     "flg_gen_noise_grid": [P, U64, I32, I32, I32, F32, P],
     "flg_version": [],
+    "flg_ply_read": [C.c_char_p, C.POINTER(FlgHostMesh), C.c_char_p, C.c_size_t],
+    "flg_grid_create_sparse": [P, P, P, I64, I32, I32, I32, C.POINTER(F32), C.POINTER(F32), C.POINTER(FlgMedium), PP],
+    "flg_grid_sparsify": [P, P, I32, I32, I32, P, P, I64, C.POINTER(I64)],
+    "flg_host_mesh_free": [C.POINTER(FlgHostMesh)],
 }
 _RESTYPE = {"flg_status_string": C.c_char_p, "flg_version": C.c_char_p, "flg_ctx_stream": C.c_void_p,
-            "flg_ctx_launch_count": C.c_int64}
+            "flg_ctx_launch_count": C.c_int64, "flg_host_mesh_free": None}
 
 _lib = None
 

@@ -130,6 +130,10 @@ struct flg_grid_t {
   flg_medium medium{};
   float sigma_t = 0.0f;
   float *d_params = nullptr;  // [0] majorant, [1] 1/majorant
+  // Sparse grids: brick table [bnz][bny][bnx] (slot or -1) over rho's bricks.
+  const int32_t *bidx = nullptr;
+  int32_t bnx = 0, bny = 0, bnz = 0;
+  int64_t n_bricks = 0;
 };
 
 struct flg_graph_t {

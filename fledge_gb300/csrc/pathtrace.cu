@@ -20,11 +20,13 @@
 // triangle is chosen uniformly and a point on it by UniformSampleTriangle
 // (math_utils.h:90-93), with the area pdf converted to solid angle.
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <vector>
 
 #include "common.cuh"
 #include "internal.h"
+#include "volume.cuh"
 
 namespace flg {
 
@@ -90,6 +92,11 @@ struct PtScene {
   float eye[3], fwd[3], right[3], up[3];
   float fov_ratio, aspect;
   int width, height, spp, max_depth;
+  // Participating medium filling the grid's box (volumetric path tracing).
+  int medium;
+  GridDev G;
+  float g;
+  uint64_t seed;
 };
 
 __device__ __forceinline__ float3 pt_vertex(const PtScene &S, int64_t tri, int k) {
@@ -179,6 +186,13 @@ __device__ __forceinline__ int queue_slot(bool want, int32_t *counter) {
   return want ? base + __popc(m & ((1u << lane) - 1u)) : -1;
 }
 
+// One path vertex per queued ray (PathIntegrator::Li, integrator.cpp:
+// 252-326; with a medium, VolPathIntegrator::Li, :407-510): emission at the
+// first bounce; with a medium, delta tracking over [0, t_hit] may move the
+// vertex to a scattering point (beta *= sigma_s / sigma_t); next-event
+// estimation toward one light triangle (Lambertian or Henyey-Greenstein
+// factor; the shadow ray's transmittance is applied in k_pt_shadow); the
+// continuation ray (cosine-weighted bounce or HGSampleP).
 __global__ void __launch_bounds__(256)
     k_pt_shade(PtScene S, Halton H, int s, int depth, int64_t n_in, PtQueues Q, int qa, const int32_t *__restrict__ prim,
                const float *__restrict__ th, const float *__restrict__ uh, const float *__restrict__ vh, float *radiance) {
@@ -187,8 +201,8 @@ __global__ void __launch_bounds__(256)
   const int qb = qa ^ 1;
   int pix = 0, cnt = 0;
   bool cont = false, shadow = false;
-  float3 o = make_float3(0.f, 0.f, 0.f), d = o, p = o, ng = o, beta = make_float3(1.f, 1.f, 1.f);
-  float3 so = o, sd = o, contrib = o, nd = o;
+  float3 o = make_float3(0.f, 0.f, 0.f), d = o, beta = make_float3(1.f, 1.f, 1.f);
+  float3 so = o, sd = o, contrib = o, nd = o, no = o;
   float smax = 0.0f;
   const float inv_spp = 1.0f / (float)S.spp;
   if (valid) {
@@ -204,8 +218,9 @@ __global__ void __launch_bounds__(256)
     if (h >= 0) {
       const float3 a = pt_vertex(S, h, 0), b = pt_vertex(S, h, 1), c = pt_vertex(S, h, 2);
       const float u = uh[q], v = vh[q], w = 1.0f - u - v;
-      p = make_float3(w * a.x + u * b.x + v * c.x, w * a.y + u * b.y + v * c.y, w * a.z + u * b.z + v * c.z);
-      ng = f3norm(f3cross(f3sub(b, a), f3sub(c, a)));
+      const float3 p = make_float3(w * a.x + u * b.x + v * c.x, w * a.y + u * b.y + v * c.y,
+                                   w * a.z + u * b.z + v * c.z);
+      const float3 ng = f3norm(f3cross(f3sub(b, a), f3sub(c, a)));
       const bool is_light = h >= S.light_first && h < S.light_first + S.light_count;
       // emission seen directly (bounces == 0); AreaLight::L (light.cpp:76-79)
       if (depth == 0 && is_light && f3dot(ng, make_float3(-d.x, -d.y, -d.z)) > 0.0f) {
@@ -214,6 +229,19 @@ __global__ void __launch_bounds__(256)
         atomicAdd(radiance + 3 * pix + 2, beta.z * S.le[2] * inv_spp);
       }
       if (depth < S.max_depth) {
+        const float3 wo = make_float3(-d.x, -d.y, -d.z);
+        // Volume::sample over the segment up to the surface (volume.cpp:109-148)
+        bool scatter = false;
+        float3 ps = p;
+        if (S.medium) {
+          RayStream rs;
+          rs.init(S.seed, path_stream_id(pix, s, depth, 0), 0u);
+          scatter = delta_track(S.G, __ldg(S.G.params), o, d, th[q], rs, ps);
+          if (scatter) {
+            const float wgt = S.G.sigma_s / S.G.sigma_t;
+            beta = make_float3(beta.x * wgt, beta.y * wgt, beta.z * wgt);
+          }
+        }
         // UniformSampleOneLight / EstimateDirect
         const float ul = halton(H, index, cnt);
         const float ua = halton(H, index, cnt + 1), ub = halton(H, index, cnt + 2);
@@ -229,55 +257,70 @@ __global__ void __launch_bounds__(256)
         const float3 lcr = f3cross(f3sub(lb, la), f3sub(lc, la));
         const float area = 0.5f * sqrtf(f3dot(lcr, lcr));
         const float3 ln = f3scale(lcr, 1.0f / (2.0f * area));
-        const float3 toL = f3sub(lp, p);
+        const float3 toL = f3sub(lp, ps);
         const float dist = sqrtf(f3dot(toL, toL));
         const float3 wi = f3scale(toL, 1.0f / dist);
         const float cos_l = -f3dot(ln, wi);
         if (cos_l > 0.0f && dist > 0.0f) {
           const float pdf = dist * dist / (cos_l * area);
-          const float cos_s = fabsf(f3dot(wi, ng));
-          const float k = cos_s * (1.0f / 3.14159265358979f) / (pdf * light_pdf) * inv_spp;
-          contrib = make_float3(beta.x * S.albedo[0] * S.le[0] * k, beta.y * S.albedo[1] * S.le[1] * k,
-                                beta.z * S.albedo[2] * S.le[2] * k);
-          so = offset_origin(p, ng, wi);
+          float3 f;
+          if (scatter) {
+            const float ph = hg_p(wi, wo, S.g);
+            f = make_float3(ph, ph, ph);
+          } else {
+            const float cos_s = fabsf(f3dot(wi, ng));
+            f = make_float3(S.albedo[0] * (1.0f / 3.14159265358979f) * cos_s,
+                            S.albedo[1] * (1.0f / 3.14159265358979f) * cos_s,
+                            S.albedo[2] * (1.0f / 3.14159265358979f) * cos_s);
+          }
+          const float k = inv_spp / (pdf * light_pdf);
+          contrib = make_float3(beta.x * f.x * S.le[0] * k, beta.y * f.y * S.le[1] * k, beta.z * f.z * S.le[2] * k);
+          so = scatter ? ps : offset_origin(p, ng, wi);  // a medium vertex has no normal to offset along
           sd = wi;
           smax = dist - 1e-4f;  // SpawnRayTo: tMax = |p' - p| - SHADOW_EPS
           shadow = contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f;
         }
-        // Lambertian sampleF in the frame of the normal (material_base.hpp:14-41)
         const float u1 = halton(H, index, cnt), u2 = halton(H, index, cnt + 1);
         cnt += 2;
-        float3 bn;
-        if (fabsf(ng.x) > fabsf(ng.z)) bn = make_float3(-ng.y, ng.x, 0.0f);
-        else bn = make_float3(0.0f, -ng.z, ng.y);
-        bn = f3norm(bn);
-        const float3 tg = f3cross(bn, ng);
-        const float3 wo = make_float3(-d.x, -d.y, -d.z);
-        const float woz = f3dot(wo, ng);
-        // CosineSampleHemisphere (ConcentricSampleDisk, math_utils.h:69-88)
-        const float ux = u1 * 2.0f - 1.0f, uy = u2 * 2.0f - 1.0f;
-        float dx = 0.0f, dy = 0.0f;
-        if (ux != 0.0f || uy != 0.0f) {
-          float r, theta;
-          if (fabsf(ux) > fabsf(uy)) {
-            r = ux;
-            theta = 0.78539816f * (uy / ux);
-          } else {
-            r = uy;
-            theta = 1.57079633f - 0.78539816f * (ux / uy);
-          }
-          dx = cosf(theta) * r;
-          dy = sinf(theta) * r;
-        }
-        const float dz = sqrtf(fmaxf(0.0f, 1.0f - dx * dx - dy * dy));
-        const float pdf_b = woz * dz > 0.0f ? fabsf(dz) * (1.0f / 3.14159265358979f) : 0.0f;
-        if (pdf_b > 0.0f) {
-          nd = make_float3(tg.x * dx + bn.x * dy + ng.x * dz, tg.y * dx + bn.y * dy + ng.y * dz,
-                           tg.z * dx + bn.z * dy + ng.z * dz);
-          const float fcos = (1.0f / 3.14159265358979f) * fabsf(f3dot(nd, ng)) / pdf_b;
-          beta = make_float3(beta.x * S.albedo[0] * fcos, beta.y * S.albedo[1] * fcos, beta.z * S.albedo[2] * fcos);
-          nd = f3norm(nd);
+        if (scatter) {
+          // HGSampleP: the phase function and its pdf cancel in beta
+          nd = hg_sample(wo, u1, u2, S.g);
+          no = ps;
           cont = true;
+        } else {
+          // Lambertian sampleF in the frame of the normal (material_base.hpp:14-41)
+          float3 bn;
+          if (fabsf(ng.x) > fabsf(ng.z)) bn = make_float3(-ng.y, ng.x, 0.0f);
+          else bn = make_float3(0.0f, -ng.z, ng.y);
+          bn = f3norm(bn);
+          const float3 tg = f3cross(bn, ng);
+          const float woz = f3dot(wo, ng);
+          // CosineSampleHemisphere (ConcentricSampleDisk, math_utils.h:69-88)
+          const float ux = u1 * 2.0f - 1.0f, uy = u2 * 2.0f - 1.0f;
+          float dx = 0.0f, dy = 0.0f;
+          if (ux != 0.0f || uy != 0.0f) {
+            float r, theta;
+            if (fabsf(ux) > fabsf(uy)) {
+              r = ux;
+              theta = 0.78539816f * (uy / ux);
+            } else {
+              r = uy;
+              theta = 1.57079633f - 0.78539816f * (ux / uy);
+            }
+            dx = cosf(theta) * r;
+            dy = sinf(theta) * r;
+          }
+          const float dz = sqrtf(fmaxf(0.0f, 1.0f - dx * dx - dy * dy));
+          const float pdf_b = woz * dz > 0.0f ? fabsf(dz) * (1.0f / 3.14159265358979f) : 0.0f;
+          if (pdf_b > 0.0f) {
+            nd = make_float3(tg.x * dx + bn.x * dy + ng.x * dz, tg.y * dx + bn.y * dy + ng.y * dz,
+                             tg.z * dx + bn.z * dy + ng.z * dz);
+            const float fcos = (1.0f / 3.14159265358979f) * fabsf(f3dot(nd, ng)) / pdf_b;
+            beta = make_float3(beta.x * S.albedo[0] * fcos, beta.y * S.albedo[1] * fcos, beta.z * S.albedo[2] * fcos);
+            nd = f3norm(nd);
+            no = offset_origin(p, ng, nd);
+            cont = true;
+          }
         }
       }
     }
@@ -295,7 +338,6 @@ __global__ void __launch_bounds__(256)
   }
   const int ns = queue_slot(valid && cont, Q.counts);
   if (ns >= 0) {
-    const float3 no = offset_origin(p, ng, nd);
     Q.rx[qb][0][ns] = no.x; Q.rx[qb][1][ns] = no.y; Q.rx[qb][2][ns] = no.z;
     Q.rx[qb][3][ns] = nd.x; Q.rx[qb][4][ns] = nd.y; Q.rx[qb][5][ns] = nd.z;
     Q.path[qb][ns] = pix;
@@ -306,14 +348,27 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-__global__ void k_pt_shadow(int64_t n, const uint8_t *__restrict__ occ, const float *__restrict__ contrib,
-                            const int32_t *__restrict__ spix, float *radiance) {
+// Unoccluded shadow rays add their contribution; with a medium, times the
+// ratio-tracking transmittance of the shadow segment (VolEstimateTr,
+// integrator.cpp:40-66).
+__global__ void k_pt_shadow(PtScene S, int s, int depth, int64_t n, const uint8_t *__restrict__ occ, PtQueues Q,
+                            float *radiance) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || occ[i]) return;
-  const int p = spix[i];
-  atomicAdd(radiance + 3 * p, contrib[3 * i]);
-  atomicAdd(radiance + 3 * p + 1, contrib[3 * i + 1]);
-  atomicAdd(radiance + 3 * p + 2, contrib[3 * i + 2]);
+  const int p = Q.spix[i];
+  float tr = 1.0f;
+  if (S.medium) {
+    const float3 o = make_float3(Q.sx[0][i], Q.sx[1][i], Q.sx[2][i]);
+    const float3 d = make_float3(Q.sx[3][i], Q.sx[4][i], Q.sx[5][i]);
+    float ct, cc;
+    uint32_t ck;
+    tr = ratio_track(S.G, __ldg(S.G.params), __ldg(S.G.params + 1), o, d, Q.sx[6][i], S.seed,
+                     (int64_t)path_stream_id(p, s, depth, 1), ct, ck, cc);
+    if (tr == 0.0f) return;
+  }
+  atomicAdd(radiance + 3 * p, Q.scontrib[3 * i] * tr);
+  atomicAdd(radiance + 3 * p + 1, Q.scontrib[3 * i + 1] * tr);
+  atomicAdd(radiance + 3 * p + 2, Q.scontrib[3 * i + 2] * tr);
 }
 
 static void host_halton(int width, int height, Halton &H) {
@@ -361,9 +416,11 @@ static void host_halton(int width, int height, Halton &H) {
 
 using namespace flg;
 
-FLG_API int flg_pathtrace(flg_ctx ctx, flg_bvh bvh, const flg_pt_scene *scene, const flg_pt_camera *cam, int32_t spp,
-                          int32_t max_depth, const flg_trace_opts *opts, float *radiance, flg_pt_stats *stats) {
+static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed, const flg_pt_scene *scene,
+                         const flg_pt_camera *cam, int32_t spp, int32_t max_depth, const flg_trace_opts *opts,
+                         float *radiance, flg_pt_stats *stats) {
   if (!ctx || !bvh || !scene || !cam || !radiance) return ctx ? set_error(ctx, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
+  if (spp > 65535 || max_depth > 255) return set_error(ctx, FLG_ERR_ARG, "spp above 65535 or depth above 255");
   if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "path tracing synchronises per bounce; not capturable");
   if (bvh->n_scenes != 1) return set_error(ctx, FLG_ERR_ARG, "path tracing takes a single-scene handle");
   if (cam->width < 1 || cam->height < 1 || spp < 1 || max_depth < 0)
@@ -373,6 +430,16 @@ FLG_API int flg_pathtrace(flg_ctx ctx, flg_bvh bvh, const flg_pt_scene *scene, c
     return set_error(ctx, FLG_ERR_ARG, "light triangles out of range");
   if ((int64_t)cam->width * cam->height > (int64_t)1 << 26) return set_error(ctx, FLG_ERR_UNSUPPORTED, "image too large");
   PtScene S;
+  S.medium = grid ? 1 : 0;
+  if (grid) {
+    if (grid->ctx != ctx) return set_error(ctx, FLG_ERR_ARG, "grid belongs to another context");
+    S.G = grid_dev(grid);
+    S.g = grid->medium.g;
+  } else {
+    std::memset(&S.G, 0, sizeof(S.G));
+    S.g = 0.0f;
+  }
+  S.seed = seed;
   S.pos = scene->pos;
   S.idx = scene->idx;
   S.light_first = scene->light_first;
@@ -472,7 +539,7 @@ FLG_API int flg_pathtrace(flg_ctx ctx, flg_bvh bvh, const flg_pt_scene *scene, c
         rc = trace_enqueue(ctx, st, 0, bvh, &sr, counts[1], opts, nullptr, 1, nullptr, occ);
         if (rc) return rc;
         n_shadow += counts[1];
-        k_pt_shadow<<<(unsigned)ceil_div(counts[1], 256), 256, 0, st>>>(counts[1], occ, Q.scontrib, Q.spix, radiance);
+        k_pt_shadow<<<(unsigned)ceil_div(counts[1], 256), 256, 0, st>>>(S, s, depth, counts[1], occ, Q, radiance);
         FLG_LAUNCH_CHECK(ctx, "k_pt_shadow");
       }
       n_a = counts[0];
@@ -484,4 +551,16 @@ FLG_API int flg_pathtrace(flg_ctx ctx, flg_bvh bvh, const flg_pt_scene *scene, c
     stats->shadow_rays = n_shadow;
   }
   return FLG_OK;
+}
+
+FLG_API int flg_pathtrace(flg_ctx ctx, flg_bvh bvh, const flg_pt_scene *scene, const flg_pt_camera *cam, int32_t spp,
+                          int32_t max_depth, const flg_trace_opts *opts, float *radiance, flg_pt_stats *stats) {
+  return pathtrace_run(ctx, bvh, nullptr, 0, scene, cam, spp, max_depth, opts, radiance, stats);
+}
+
+FLG_API int flg_volpath(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed, const flg_pt_scene *scene,
+                        const flg_pt_camera *cam, int32_t spp, int32_t max_depth, const flg_trace_opts *opts,
+                        float *radiance, flg_pt_stats *stats) {
+  if (!grid) return ctx ? set_error(ctx, FLG_ERR_ARG, "grid is NULL") : FLG_ERR_ARG;
+  return pathtrace_run(ctx, bvh, grid, seed, scene, cam, spp, max_depth, opts, radiance, stats);
 }

@@ -15,111 +15,19 @@
 
 #include "common.cuh"
 #include "internal.h"
+#include "volume.cuh"
 
 namespace flg {
-
-struct GridDev {
-  const float *rho;
-  int nx, ny, nz;
-  float lo[3], hi[3], scale[3];
-  float sigma_s, sigma_a, sigma_t, rr;
-  const float *params;  // [0] majorant, [1] 1/majorant (double quotient as float)
-};
 
 struct VRays {
   const float *ox, *oy, *oz, *dx, *dy, *dz, *tmax;
   float tmax_c;
 };
 
-__device__ __forceinline__ float gat(const GridDev &G, int x, int y, int z) {
-  if (x < 0 || y < 0 || z < 0 || x >= G.nx || y >= G.ny || z >= G.nz) return 0.0f;
-  return __ldg(G.rho + ((int64_t)z * G.ny + y) * G.nx + x);
-}
-
-__device__ __forceinline__ float lerpf(float a, float b, float w) { return a + (b - a) * w; }
-
-__device__ __forceinline__ float sample_grid(const GridDev &G, float px, float py, float pz, int &x, int &y, int &z,
-                                             float &fx, float &fy, float &fz) {
-  float gx = (px - G.lo[0]) * G.scale[0];
-  float gy = (py - G.lo[1]) * G.scale[1];
-  float gz = (pz - G.lo[2]) * G.scale[2];
-  float x0 = floorf(gx), y0 = floorf(gy), z0 = floorf(gz);
-  x = (int)x0;
-  y = (int)y0;
-  z = (int)z0;
-  fx = gx - x0;
-  fy = gy - y0;
-  fz = gz - z0;
-  float c00 = lerpf(gat(G, x, y, z), gat(G, x + 1, y, z), fx);
-  float c10 = lerpf(gat(G, x, y + 1, z), gat(G, x + 1, y + 1, z), fx);
-  float c01 = lerpf(gat(G, x, y, z + 1), gat(G, x + 1, y, z + 1), fx);
-  float c11 = lerpf(gat(G, x, y + 1, z + 1), gat(G, x + 1, y + 1, z + 1), fx);
-  float c0 = lerpf(c00, c10, fy);
-  float c1 = lerpf(c01, c11, fy);
-  return lerpf(c0, c1, fz);
-}
-
-// AABB::intersect_pbrt (common/aabb.h:38-59) with t1 starting at tMax.
-__device__ __forceinline__ bool box_pbrt(const GridDev &G, const float3 &o, const float3 &d, float tmax, float &t0o,
-                                         float &t1o) {
-  float t0 = 0.0f, t1 = tmax;
-  const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    float inv = __frcp_rn(dd[i]);
-    float tn = (G.lo[i] - oo[i]) * inv;
-    float tf = (G.hi[i] - oo[i]) * inv;
-    bool s = tn > tf;
-    float a = s ? tf : tn, b = s ? tn : tf;
-    t0 = a > t0 ? a : t0;
-    t1 = b < t1 ? b : t1;
-    if (t0 > t1) return false;
-  }
-  t0o = t0;
-  t1o = t1;
-  return true;
-}
-
 __device__ __forceinline__ void load_vray(const VRays &R, int64_t i, float3 &o, float3 &d, float &tmax) {
   o = make_float3(__ldg(R.ox + i), __ldg(R.oy + i), __ldg(R.oz + i));
   d = make_float3(__ldg(R.dx + i), __ldg(R.dy + i), __ldg(R.dz + i));
   tmax = R.tmax ? __ldg(R.tmax + i) : R.tmax_c;
-}
-
-// Ratio tracking of one ray; returns T and the state after the last
-// roulette survival.
-__device__ __forceinline__ float ratio_track(const GridDev &G, float maj, float inv_maj, const float3 &o,
-                                             const float3 &d, float tmax, uint64_t seed, int64_t ray, float &ck_t,
-                                             uint32_t &ck_k, float &ck_c) {
-  ck_t = 0.0f;
-  ck_k = 0u;
-  ck_c = 1.0f;
-  float t_min, t_max;
-  if (!box_pbrt(G, o, d, tmax, t_min, t_max)) return 1.0f;
-  float tr = 1.0f, t = fmaxf(t_min, 0.0f);
-  t_max = fminf(t_max, tmax);
-  const float max_mu = G.sigma_t * maj;
-  RayStream rs;
-  rs.init(seed, (uint64_t)ray, 0u);
-  ck_t = t;
-  for (int step_ = 0; step_ < kMaxTrackSteps; ++step_) {
-    float u = rs.next();
-    t += -flg_logf(1.0f - u) / max_mu;
-    if (t >= t_max) break;
-    int x, y, z;
-    float fx, fy, fz;
-    float dens = sample_grid(G, o.x + d.x * t, o.y + d.y * t, o.z + d.z * t, x, y, z, fx, fy, fz);
-    tr *= 1.0f - fmaxf(0.0f, dens * inv_maj);
-    if (tr < G.rr) {
-      float q = fmaxf(0.05f, 1.0f - tr);
-      if (rs.next() < q) return 0.0f;
-      tr /= 1.0f - q;
-      ck_t = t;
-      ck_k = rs.k;
-      ck_c = tr;
-    }
-  }
-  return tr;
 }
 
 __global__ void __launch_bounds__(256)
@@ -185,10 +93,10 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
-      const int X = x + cx, Y = y + cy, Z = z + cz;
-      if (X < 0 || Y < 0 || Z < 0 || X >= G.nx || Y >= G.ny || Z >= G.nz) continue;
+      const int64_t off = grid_voxel(G, x + cx, y + cy, z + cz);
+      if (off < 0) continue;  // outside, or an empty brick of a sparse grid (not a parameter)
       float w = (cx ? fx : 1.0f - fx) * (cy ? fy : 1.0f - fy) * (cz ? fz : 1.0f - fz);
-      atomicAdd(grad + ((int64_t)Z * G.ny + Y) * G.nx + X, coef * w);
+      atomicAdd(grad + off, coef * w);
     }
   }
 }
@@ -202,36 +110,11 @@ __global__ void __launch_bounds__(256)
   float3 o, d;
   float tmax;
   load_vray(R, i, o, d, tmax);
-  uint8_t ok = 0;
-  float px = 0.0f, py = 0.0f, pz = 0.0f, w = 1.0f;
-  float t_min, t_max;
-  if (box_pbrt(G, o, d, tmax, t_min, t_max)) {
-    float t = fmaxf(t_min, 0.0f);
-    const float max_mu = G.sigma_t * maj;
-    t_max = fminf(t_max, tmax);
-    RayStream rs;
-    rs.init(seed, (uint64_t)i, 0u);
-    for (int step_ = 0; step_ < kMaxTrackSteps; ++step_) {
-      float u = rs.next();
-      t += -flg_logf(1.0f - u) / max_mu;
-      if (t >= t_max) break;
-      float qx = o.x + d.x * t, qy = o.y + d.y * t, qz = o.z + d.z * t;
-      int x, y, z;
-      float fx, fy, fz;
-      float dens = sample_grid(G, qx, qy, qz, x, y, z, fx, fy, fz);
-      float p_s = G.sigma_s * dens / max_mu;
-      float p_a = G.sigma_a * dens / max_mu;
-      float p_n = 1.0f - p_s - p_a;
-      if (rs.next() > p_n) {
-        ok = 1;
-        px = qx;
-        py = qy;
-        pz = qz;
-        w = G.sigma_s / G.sigma_t;
-        break;
-      }
-    }
-  }
+  RayStream rs;
+  rs.init(seed, (uint64_t)i, 0u);
+  float3 q = make_float3(0.0f, 0.0f, 0.0f);
+  const uint8_t ok = delta_track(G, maj, o, d, tmax, rs, q) ? 1 : 0;
+  const float px = q.x, py = q.y, pz = q.z, w = ok ? G.sigma_s / G.sigma_t : 1.0f;
   success[i] = ok;
   p[3 * i] = px;
   p[3 * i + 1] = py;
@@ -257,25 +140,6 @@ __global__ void k_grid_inv(float *params) {
   params[1] = (float)(1.0 / (double)params[0]);
 }
 
-static GridDev grid_dev(flg_grid g) {
-  GridDev G;
-  G.rho = g->rho;
-  G.nx = g->nx;
-  G.ny = g->ny;
-  G.nz = g->nz;
-  for (int k = 0; k < 3; ++k) {
-    G.lo[k] = g->lo[k];
-    G.hi[k] = g->hi[k];
-    G.scale[k] = g->scale[k];
-  }
-  G.sigma_s = g->medium.sigma_s;
-  G.sigma_a = g->medium.sigma_a;
-  G.sigma_t = g->sigma_t;
-  G.rr = g->medium.rr_threshold;
-  G.params = g->d_params;
-  return G;
-}
-
 static int vrays(flg_ctx ctx, const flg_rays *r, int64_t n, VRays &V) {
   if (!r) return set_error(ctx, FLG_ERR_ARG, "rays is NULL");
   if (n < 0) return set_error(ctx, FLG_ERR_ARG, "n < 0");
@@ -285,12 +149,72 @@ static int vrays(flg_ctx ctx, const flg_rays *r, int64_t n, VRays &V) {
   return FLG_OK;
 }
 
+// Sparse grids.  One CTA of 128 threads per brick; a brick is kept when one
+// of its voxels differs from +0 (background), and keeps its slot in brick
+// order (k_brick_scan), so the layout is deterministic.
+__global__ void k_brick_flags(const float *__restrict__ rho, int nx, int ny, int nz, int bnx, int bny,
+                              int32_t *__restrict__ bidx) {
+  const int64_t b = blockIdx.x;
+  const int bx = (int)(b % bnx), by = (int)((b / bnx) % bny), bz = (int)(b / ((int64_t)bnx * bny));
+  int any = 0;
+  for (int v = threadIdx.x; v < kBrick * kBrick * kBrick; v += blockDim.x) {
+    const int x = bx * kBrick + v % kBrick, y = by * kBrick + (v / kBrick) % kBrick, z = bz * kBrick + v / (kBrick * kBrick);
+    if (x < nx && y < ny && z < nz && __float_as_uint(rho[((int64_t)z * ny + y) * nx + x]) != 0u) any = 1;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) bidx[b] = any;
+}
+
+// Exclusive scan of the 0/1 flags into slots (-1 for empty bricks), one CTA.
+__global__ void k_brick_scan(int32_t *bidx, int64_t nb, int64_t *count) {
+  __shared__ int64_t s_part[1024];
+  const int t = threadIdx.x;
+  const int64_t per = (nb + blockDim.x - 1) / blockDim.x;
+  const int64_t a = t * per, e = min(a + per, nb);
+  int64_t c = 0;
+  for (int64_t i = a; i < e; ++i) c += bidx[i];
+  s_part[t] = c;
+  __syncthreads();
+  if (t == 0) {
+    int64_t run = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      const int64_t x = s_part[i];
+      s_part[i] = run;
+      run += x;
+    }
+    *count = run;
+  }
+  __syncthreads();
+  int64_t run = s_part[t];
+  for (int64_t i = a; i < e; ++i) {
+    const int32_t f = bidx[i];
+    bidx[i] = f ? (int32_t)run : -1;
+    run += f;
+  }
+}
+
+__global__ void k_brick_copy(const float *__restrict__ rho, int nx, int ny, int nz, int bnx, int bny,
+                             const int32_t *__restrict__ bidx, float *__restrict__ bricks) {
+  const int64_t b = blockIdx.x;
+  const int32_t slot = bidx[b];
+  if (slot < 0) return;
+  const int bx = (int)(b % bnx), by = (int)((b / bnx) % bny), bz = (int)(b / ((int64_t)bnx * bny));
+  for (int v = threadIdx.x; v < kBrick * kBrick * kBrick; v += blockDim.x) {
+    const int x = bx * kBrick + v % kBrick, y = by * kBrick + (v / kBrick) % kBrick, z = bz * kBrick + v / (kBrick * kBrick);
+    const float val = (x < nx && y < ny && z < nz) ? rho[((int64_t)z * ny + y) * nx + x] : 0.0f;
+    bricks[(int64_t)slot * (kBrick * kBrick * kBrick) + v] = val;
+  }
+}
+
 }  // namespace flg
 
 using namespace flg;
 
-FLG_API int flg_grid_create(flg_ctx ctx, const float *density, int32_t nx, int32_t ny, int32_t nz,
-                            const float *lo, const float *hi, const flg_medium *medium, flg_grid *out) {
+// Shared by the dense and the sparse constructors: rho holds nv values (the
+// dense lattice, or the bricks), over which the majorant is taken.
+static int grid_new(flg_ctx ctx, const float *density, int64_t nv, const int32_t *bidx, int64_t n_bricks,
+                    int32_t nx, int32_t ny, int32_t nz, const float *lo, const float *hi, const flg_medium *medium,
+                    flg_grid *out) {
   if (!ctx || !out) return FLG_ERR_ARG;
   *out = nullptr;
   if (!density || !lo || !hi || !medium) return set_error(ctx, FLG_ERR_ARG, "NULL argument");
@@ -303,6 +227,11 @@ FLG_API int flg_grid_create(flg_ctx ctx, const float *density, int32_t nx, int32
   flg_grid g = new flg_grid_t();
   g->ctx = ctx;
   g->rho = density;
+  g->bidx = bidx;
+  g->n_bricks = n_bricks;
+  g->bnx = (nx + kBrick - 1) / kBrick;
+  g->bny = (ny + kBrick - 1) / kBrick;
+  g->bnz = (nz + kBrick - 1) / kBrick;
   g->nx = nx;
   g->ny = ny;
   g->nz = nz;
@@ -327,8 +256,7 @@ FLG_API int flg_grid_create(flg_ctx ctx, const float *density, int32_t nx, int32
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   } else {
     e = cudaMemsetAsync(g->d_params, 0, 4 * sizeof(float), st);
-    const int64_t nv = (int64_t)nx * ny * nz;
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && nv > 0) {
       k_grid_max<<<grid_for(nv, 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(density, nv, g->d_params);
       k_grid_inv<<<1, 1, 0, st>>>(g->d_params);
       e = cudaGetLastError();
@@ -340,6 +268,56 @@ FLG_API int flg_grid_create(flg_ctx ctx, const float *density, int32_t nx, int32
     return cuda_fail(ctx, e, "grid create");
   }
   *out = g;
+  return FLG_OK;
+}
+
+FLG_API int flg_grid_create(flg_ctx ctx, const float *density, int32_t nx, int32_t ny, int32_t nz,
+                            const float *lo, const float *hi, const flg_medium *medium, flg_grid *out) {
+  return grid_new(ctx, density, (int64_t)nx * ny * nz, nullptr, 0, nx, ny, nz, lo, hi, medium, out);
+}
+
+FLG_API int flg_grid_create_sparse(flg_ctx ctx, const int32_t *brick_index, const float *bricks, int64_t n_bricks,
+                                   int32_t nx, int32_t ny, int32_t nz, const float *lo, const float *hi,
+                                   const flg_medium *medium, flg_grid *out) {
+  if (!ctx) return FLG_ERR_ARG;
+  if (!brick_index) return set_error(ctx, FLG_ERR_ARG, "brick_index is NULL");
+  if (n_bricks < 0 || (n_bricks > 0 && !bricks)) return set_error(ctx, FLG_ERR_ARG, "bad brick array");
+  static const float kNoBricks[1] = {0.0f};  // never read: every slot is -1
+  return grid_new(ctx, n_bricks > 0 ? bricks : kNoBricks, n_bricks * kBrick * kBrick * kBrick, brick_index,
+                  n_bricks, nx, ny, nz, lo, hi, medium, out);
+}
+
+FLG_API int flg_grid_sparsify(flg_ctx ctx, const float *density, int32_t nx, int32_t ny, int32_t nz,
+                              int32_t *brick_index, float *bricks, int64_t max_bricks, int64_t *n_bricks) {
+  if (!ctx || !n_bricks) return FLG_ERR_ARG;
+  if (!density || !brick_index) return set_error(ctx, FLG_ERR_ARG, "NULL argument");
+  if (nx < 1 || ny < 1 || nz < 1) return set_error(ctx, FLG_ERR_ARG, "bad grid size");
+  if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "sparsify reads its count back to the host");
+  const int bnx = (nx + kBrick - 1) / kBrick, bny = (ny + kBrick - 1) / kBrick, bnz = (nz + kBrick - 1) / kBrick;
+  const int64_t nb = (int64_t)bnx * bny * bnz;
+  if (nb > ((int64_t)1 << 31) - 1) return set_error(ctx, FLG_ERR_UNSUPPORTED, "too many bricks");
+  cudaStream_t st = ctx->stream;
+  int64_t *d_count = nullptr;
+  FLG_CUDA(ctx, cudaMalloc((void **)&d_count, sizeof(int64_t)));
+  k_brick_flags<<<(unsigned)nb, kBrick * kBrick * kBrick / 4, 0, st>>>(density, nx, ny, nz, bnx, bny, brick_index);
+  cudaError_t e = cudaGetLastError();
+  ++ctx->launches;
+  if (e == cudaSuccess) {
+    k_brick_scan<<<1, 1024, 0, st>>>(brick_index, nb, d_count);
+    e = cudaGetLastError();
+    ++ctx->launches;
+  }
+  int64_t count = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&count, d_count, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_count);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "sparsify");
+  *n_bricks = count;
+  if (!bricks) return FLG_OK;  // counting call
+  if (count > max_bricks) return set_error(ctx, FLG_ERR_ARG, "brick array too small (%lld bricks)", (long long)count);
+  k_brick_copy<<<(unsigned)nb, kBrick * kBrick * kBrick / 4, 0, st>>>(density, nx, ny, nz, bnx, bny, brick_index,
+                                                                       bricks);
+  FLG_LAUNCH_CHECK(ctx, "k_brick_copy");
   return FLG_OK;
 }
 

@@ -236,6 +236,22 @@ typedef struct flg_medium {
 FLG_API int flg_grid_create(flg_ctx ctx, const float *density, int32_t nx, int32_t ny, int32_t nz,
                             const float *box_lo_host, const float *box_hi_host,
                             const flg_medium *medium, flg_grid *out);
+/* Sparse grid (the NanoVDBVolume that src/volume.hpp:72-92 declares but does
+ * not implement): the lattice is cut into 8^3 bricks; brick_index (device,
+ * [ceil(nz/8)][ceil(ny/8)][ceil(nx/8)] int32) holds each brick's slot in
+ * bricks (device, n_bricks x 512 floats, z, y, x inside a brick, x fastest)
+ * or -1 for a brick of background (0) values.  Lookups, tracking, sampling
+ * and the adjoint behave exactly as on the dense grid with those values;
+ * adjoint gradients are written in the bricks' layout (empty bricks are not
+ * parameters).  Both arrays are borrowed. */
+FLG_API int flg_grid_create_sparse(flg_ctx ctx, const int32_t *brick_index, const float *bricks,
+                                   int64_t n_bricks, int32_t nx, int32_t ny, int32_t nz, const float *lo,
+                                   const float *hi, const flg_medium *medium, flg_grid *out);
+/* Converts a dense device grid into that layout: fills brick_index, stores
+ * the count of non-empty bricks in *n_bricks (host) and, when bricks is not
+ * NULL, copies them (max_bricks slots available).  Synchronises. */
+FLG_API int flg_grid_sparsify(flg_ctx ctx, const float *density, int32_t nx, int32_t ny, int32_t nz,
+                              int32_t *brick_index, float *bricks, int64_t max_bricks, int64_t *n_bricks);
 FLG_API int flg_grid_destroy(flg_grid grid);
 FLG_API int flg_grid_majorant(flg_grid grid, float *majorant_host);
 
@@ -299,6 +315,37 @@ typedef struct flg_pt_stats {
 FLG_API int flg_pathtrace(flg_ctx ctx, flg_bvh bvh, const flg_pt_scene *scene, const flg_pt_camera *cam,
                           int32_t spp, int32_t max_depth, const flg_trace_opts *opts, float *radiance,
                           flg_pt_stats *stats);
+
+/* Volumetric path tracing (VolPathIntegrator::Li, src/integrator.cpp:407-510):
+ * flg_pathtrace with the grid's medium filling the grid's box.  At each
+ * surface hit, delta tracking over the segment may move the path vertex to
+ * a scattering point (Henyey-Greenstein with the grid's g; beta *= sigma_s /
+ * sigma_t); shadow rays are weighted by ratio-tracking transmittance
+ * (VolEstimateTr, :40-66).  Tracking draws from Philox streams keyed by seed,
+ * pixel, sample, bounce and purpose.  spp <= 65535, max_depth <= 255. */
+FLG_API int flg_volpath(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed, const flg_pt_scene *scene,
+                        const flg_pt_camera *cam, int32_t spp, int32_t max_depth, const flg_trace_opts *opts,
+                        float *radiance, flg_pt_stats *stats);
+
+/* ---------------------------- mesh ingestion ---------------------------- */
+
+/* A host mesh read from a file; arrays are malloc'ed by the library and
+ * released by flg_host_mesh_free.  normal / uv are NULL when the file has
+ * none. */
+typedef struct flg_host_mesh {
+  float *pos;     /* 3 * n_vert */
+  float *normal;  /* 3 * n_vert or NULL */
+  float *uv;      /* 2 * n_vert or NULL */
+  int32_t *idx;   /* 3 * n_tri */
+  int64_t n_vert, n_tri;
+} flg_host_mesh;
+
+/* Reads a PLY file (ASCII or binary) into a triangle mesh; replaces
+ * MakeTriangleMesh (src/plymesh.cpp:19-86).  Faces with more than three
+ * corners are fan-triangulated.  Host only (no context, no GPU).  On error
+ * returns FLG_ERR_ARG and writes a message into err (err_len bytes). */
+FLG_API int flg_ply_read(const char *path, flg_host_mesh *out, char *err, size_t err_len);
+FLG_API void flg_host_mesh_free(flg_host_mesh *mesh);
 
 /* ----------------------------- CUDA graphs ------------------------------ */
 

@@ -1242,15 +1242,89 @@ V3 offset_origin(V3 p, V3 n, V3 d) {
 
 }  // namespace
 
+namespace {
+
+// Delta tracking over [0, tmax] (volume.cpp:109-148); true on a real
+// collision, position in p.
+bool delta_track(const Grid &G, const float *o, const float *d, float tmax, RayStream &rs, float *p) {
+  float t_min, t_max;
+  if (!box_intersect_pbrt(G, o, d, tmax, &t_min, &t_max)) return false;
+  float t = std::max(t_min, 0.0f);
+  const float max_mu = G.sigma_t * G.maxd;
+  t_max = std::min(t_max, tmax);
+  for (int step_ = 0; step_ < kMaxTrackSteps; ++step_) {
+    float u = rs.next();
+    t += -flg_logf(1.0f - u) / max_mu;
+    if (t >= t_max) break;
+    float pos[3] = {o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t};
+    int b[3];
+    float f[3];
+    float density = G.sample(pos, b, f);
+    float p_s = G.sigma_s * density / max_mu;
+    float p_a = G.sigma_a * density / max_mu;
+    float p_n = 1.0f - p_s - p_a;
+    if (rs.next() > p_n) {
+      p[0] = pos[0]; p[1] = pos[1]; p[2] = pos[2];
+      return true;
+    }
+  }
+  return false;
+}
+
+float hg_p(V3 wi, V3 wo, float g) {  // HGP (math_utils.h:103-107)
+  const float cos_theta = wi.x * wo.x + wi.y * wo.y + wi.z * wo.z;
+  const float denom = 1.0f + g * g + 2.0f * g * cos_theta;
+  return (1.0f - g * g) / (denom * std::sqrt(denom)) * 0.07957747154594766788f;
+}
+
+V3 hg_sample(V3 wo, float u, float v, float g) {  // HGSampleP (math_utils.h:111-128)
+  float cos_theta;
+  if (std::fabs(g) < 1e-3f) {
+    cos_theta = 1.0f - 2.0f * u;
+  } else {
+    const float tmp = (1.0f - g * g) / (1.0f + g - 2.0f * g * u);
+    cos_theta = -(1.0f + g * g - tmp * tmp) / (2.0f * g);
+  }
+  const float phi = 2.0f * 3.14159265358979f * v;
+  const float sin_theta = std::sqrt(std::max(0.0f, 1.0f - cos_theta * cos_theta));
+  V3 v1;
+  if (std::fabs(wo.x) > std::fabs(wo.y)) {  // CoordinateSystem (math_utils.h:57-66)
+    const float l = std::sqrt(wo.x * wo.x + wo.z * wo.z);
+    v1 = v3(-wo.z / l, 0.0f, wo.x / l);
+  } else {
+    const float l = std::sqrt(wo.y * wo.y + wo.z * wo.z);
+    v1 = v3(0.0f, wo.z / l, -wo.y / l);
+  }
+  const V3 v2 = cross(wo, v1);
+  const float a = sin_theta * std::cos(phi), b = sin_theta * std::sin(phi);
+  return v3(a * v1.x + b * v2.x + cos_theta * wo.x, a * v1.y + b * v2.y + cos_theta * wo.y,
+            a * v1.z + b * v2.z + cos_theta * wo.z);
+}
+
+inline uint64_t path_stream_id(int64_t pix, int s, int depth, int purpose) {
+  return (uint64_t)pix | ((uint64_t)s << 26) | ((uint64_t)depth << 42) | ((uint64_t)purpose << 50);
+}
+
+}  // namespace
+
+// PathIntegrator::Li (integrator.cpp:252-326) per pixel in eval_pixel's sample
+// order (:136-159); with a grid (rho != NULL), VolPathIntegrator::Li
+// (:407-510) with the medium filling the grid's box: delta tracking over the
+// segment up to each surface hit, Henyey-Greenstein scattering, shadow rays
+// weighted by ratio tracking (VolEstimateTr, :40-66).
 ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, const int32_t *perm,
                            const int32_t *split, const uint8_t *leaf, const float *nb, int32_t light_first,
                            int32_t light_count, const float *le, const float *albedo, const float *eye,
                            const float *target, const float *up, float fov_deg, int32_t width, int32_t height,
                            int32_t spp, int32_t max_depth, int32_t pixel_stride, float *radiance,
-                           int64_t *rays) {
+                           int64_t *rays, const float *rho, int32_t gnx, int32_t gny, int32_t gnz,
+                           const float *glo, const float *ghi, const OrcMedium *gm, uint64_t seed) {
   Mesh M{pos, idx, n_tri};
   Tree T{n_tri, perm, split, leaf, nb};
   HaltonH H(width, height);
+  const bool medium = rho != nullptr;
+  Grid G{};
+  if (medium) G = make_grid(rho, gnx, gny, gnz, glo, ghi, gm);
   float f[3] = {target[0] - eye[0], target[1] - eye[1], target[2] - eye[2]};
   auto nrm = [](float *v) {
     const float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
@@ -1264,6 +1338,7 @@ ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, 
   const float fov_ratio = std::tan(3.14159265358979f * fov_deg / 360.0f);
   const float aspect = (float)width / (float)height;
   const float inv_spp = 1.0f / (float)spp;
+  const float inv_pi = 1.0f / 3.14159265358979f;
   int64_t n_closest = 0, n_shadow = 0;
   const int64_t npix = (int64_t)width * height;
 #pragma omp parallel for schedule(dynamic, 16) reduction(+ : n_closest, n_shadow)
@@ -1313,6 +1388,19 @@ ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, 
         if (depth == 0 && is_light && dot(ng, v3(-D.x, -D.y, -D.z)) > 0.0f)
           for (int k = 0; k < 3; ++k) acc[k] += (double)(beta[k] * le[k] * inv_spp);
         if (depth >= max_depth) break;
+        const V3 wo = v3(-D.x, -D.y, -D.z);
+        bool scatter = false;
+        V3 ps = p;
+        if (medium) {
+          RayStream rs = stream_for(seed, (int64_t)path_stream_id(pix, s, depth, 0));
+          float q[3];
+          scatter = delta_track(G, ray.o, ray.d, b.tfar, rs, q);
+          if (scatter) {
+            ps = v3(q[0], q[1], q[2]);
+            const float wgt = G.sigma_s / G.sigma_t;
+            for (int k = 0; k < 3; ++k) beta[k] = beta[k] * wgt;
+          }
+        }
         const float ul = H.sample(index, cnt), ua = H.sample(index, cnt + 1), ub = H.sample(index, cnt + 2);
         cnt += 3;
         const int li = std::min((int)(ul * (float)light_count), light_count - 1);
@@ -1326,18 +1414,25 @@ ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, 
         const V3 lcr = cross(sub(lb, la), sub(lc, la));
         const float area = 0.5f * std::sqrt(dot(lcr, lcr));
         const V3 ln = scale3(lcr, 1.0f / (2.0f * area));
-        const V3 toL = sub(lp, p);
+        const V3 toL = sub(lp, ps);
         const float dist = std::sqrt(dot(toL, toL));
         const V3 wi = scale3(toL, 1.0f / dist);
         const float cos_l = -dot(ln, wi);
         if (cos_l > 0.0f && dist > 0.0f) {
           const float pdf = dist * dist / (cos_l * area);
-          const float cos_s = std::fabs(dot(wi, ng));
-          const float k = cos_s * (1.0f / 3.14159265358979f) / (pdf * light_pdf) * inv_spp;
-          const float ct[3] = {beta[0] * albedo[0] * le[0] * k, beta[1] * albedo[1] * le[1] * k,
-                               beta[2] * albedo[2] * le[2] * k};
+          float fv[3];
+          if (scatter) {
+            const float ph = hg_p(wi, wo, G.g);
+            fv[0] = fv[1] = fv[2] = ph;
+          } else {
+            const float cos_s = std::fabs(dot(wi, ng));
+            for (int k = 0; k < 3; ++k) fv[k] = albedo[k] * inv_pi * cos_s;
+          }
+          const float kk = inv_spp / (pdf * light_pdf);
+          float ct[3];
+          for (int k = 0; k < 3; ++k) ct[k] = beta[k] * fv[k] * le[k] * kk;
           if (ct[0] > 0.0f || ct[1] > 0.0f || ct[2] > 0.0f) {
-            const V3 so = offset_origin(p, ng, wi);
+            const V3 so = scatter ? ps : offset_origin(p, ng, wi);
             RayIn sr;
             sr.o[0] = so.x; sr.o[1] = so.y; sr.o[2] = so.z;
             sr.d[0] = wi.x; sr.d[1] = wi.y; sr.d[2] = wi.z;
@@ -1345,16 +1440,28 @@ ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, 
             sr.tmin = 1e-30f;
             sr.tmax = dist - 1e-4f;
             ++n_shadow;
-            if (!recursive_occluded(T, M, 0, sr, MODE_DEV))
-              for (int q = 0; q < 3; ++q) acc[q] += (double)ct[q];
+            if (!recursive_occluded(T, M, 0, sr, MODE_DEV)) {
+              float tr = 1.0f;
+              if (medium) {
+                RayStream rs = stream_for(seed, (int64_t)path_stream_id(pix, s, depth, 1));
+                tr = ratio_track(G, sr.o, sr.d, sr.tmax, rs, nullptr);
+              }
+              if (tr != 0.0f)
+                for (int q = 0; q < 3; ++q) acc[q] += (double)(ct[q] * tr);
+            }
           }
         }
         const float u1 = H.sample(index, cnt), u2 = H.sample(index, cnt + 1);
         cnt += 2;
+        if (scatter) {
+          D = hg_sample(wo, u1, u2, G.g);
+          O = ps;
+          continue;
+        }
         V3 bn = std::fabs(ng.x) > std::fabs(ng.z) ? v3(-ng.y, ng.x, 0.0f) : v3(0.0f, -ng.z, ng.y);
         bn = norm3(bn);
         const V3 tg = cross(bn, ng);
-        const float woz = dot(v3(-D.x, -D.y, -D.z), ng);
+        const float woz = dot(wo, ng);
         const float ux = u1 * 2.0f - 1.0f, uy = u2 * 2.0f - 1.0f;
         float dx = 0.0f, dy = 0.0f;
         if (ux != 0.0f || uy != 0.0f) {
