@@ -42,6 +42,11 @@ SEED_C0, SEED_C2, SEED_C3 = 0xF1ED0000, 0xF1ED0002, 0xF1ED0003
 # (scene, code) keys (histogram 8 + 5 passes x 24) + Karras 20 + refit 100.
 BYTES_PER_RAY = 24 + 16
 BYTES_PER_TRI_BATCHED = 36 + 44 + (8 + 5 * 24) + 20 + 100
+# DRAM bytes per ray of the trace kernel from the committed ncu capture
+# (profiles/k_trace_ww_w4_config3_8scenes.md: dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch over the first 8 scenes, divided by its
+# 41,186,368 rays); scaled by rays to a full launch.
+TRACE_DRAM_BYTES_PER_RAY_NCU = (2.409362e9 + 1.011523e9) / 41186368
 
 
 _T0 = time.perf_counter()
@@ -277,7 +282,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     trace_bytes = n_rays * BYTES_PER_RAY + int(bb.info().device_bytes)
     tr_ms = statistics.median(trace_ms)
     roof = {"bound": "hbm", "achieved": round(trace_bytes / (tr_ms * 1e-3) / 1e9, 1), "peak": pk["hbm_gbs"],
-            "unit": "GB/s", "frac": None, "traffic": None,
+            "unit": "GB/s", "frac": None,
+            "traffic": (round(n_rays * TRACE_DRAM_BYTES_PER_RAY_NCU) if width == 4 and args.persistent == 2
+                        else None),
+            "traffic_source": "ncu capture of 8 scenes scaled by rays (lower bound at full size)",
             "kernel": ("k_trace_bvh2<false>" if width == 2 else
                        f"k_trace_ww<{width},false,{args.stack}>" if args.persistent == 2 else
                        f"k_trace_persistent<{width},false,{args.stack}>" if args.persistent else

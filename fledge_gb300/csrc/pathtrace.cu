@@ -236,7 +236,8 @@ __global__ void __launch_bounds__(256)
         if (S.medium) {
           RayStream rs;
           rs.init(S.seed, path_stream_id(pix, s, depth, 0), 0u);
-          scatter = delta_track(S.G, __ldg(S.G.params), o, d, th[q], rs, ps);
+          scatter = S.G.bidx ? delta_track<true>(S.G, __ldg(S.G.params), o, d, th[q], rs, ps)
+                             : delta_track<false>(S.G, __ldg(S.G.params), o, d, th[q], rs, ps);
           if (scatter) {
             const float wgt = S.G.sigma_s / S.G.sigma_t;
             beta = make_float3(beta.x * wgt, beta.y * wgt, beta.z * wgt);
@@ -362,8 +363,11 @@ __global__ void k_pt_shadow(PtScene S, int s, int depth, int64_t n, const uint8_
     const float3 d = make_float3(Q.sx[3][i], Q.sx[4][i], Q.sx[5][i]);
     float ct, cc;
     uint32_t ck;
-    tr = ratio_track(S.G, __ldg(S.G.params), __ldg(S.G.params + 1), o, d, Q.sx[6][i], S.seed,
-                     (int64_t)path_stream_id(p, s, depth, 1), ct, ck, cc);
+    const int64_t id = (int64_t)path_stream_id(p, s, depth, 1);
+    tr = S.G.bidx ? ratio_track<true>(S.G, __ldg(S.G.params), __ldg(S.G.params + 1), o, d, Q.sx[6][i], S.seed, id,
+                                      ct, ck, cc)
+                  : ratio_track<false>(S.G, __ldg(S.G.params), __ldg(S.G.params + 1), o, d, Q.sx[6][i], S.seed, id,
+                                       ct, ck, cc);
     if (tr == 0.0f) return;
   }
   atomicAdd(radiance + 3 * p, Q.scontrib[3 * i] * tr);

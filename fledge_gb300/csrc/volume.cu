@@ -30,6 +30,7 @@ __device__ __forceinline__ void load_vray(const VRays &R, int64_t i, float3 &o, 
   tmax = R.tmax ? __ldg(R.tmax + i) : R.tmax_c;
 }
 
+template <bool SP>
 __global__ void __launch_bounds__(256)
     k_volume_tr(GridDev G, VRays R, int64_t n, uint64_t seed, float *__restrict__ T, float *__restrict__ ck_t,
                 uint32_t *__restrict__ ck_k, float *__restrict__ ck_c) {
@@ -41,7 +42,7 @@ __global__ void __launch_bounds__(256)
   load_vray(R, i, o, d, tmax);
   float ct, cc;
   uint32_t ck;
-  T[i] = ratio_track(G, maj, inv_maj, o, d, tmax, seed, i, ct, ck, cc);
+  T[i] = ratio_track<SP>(G, maj, inv_maj, o, d, tmax, seed, i, ct, ck, cc);
   if (ck_t) {
     ck_t[i] = ct;
     ck_k[i] = ck;
@@ -51,6 +52,7 @@ __global__ void __launch_bounds__(256)
 
 // Adjoint: T = c * prod_{last segment} (1 - d_i/rho_max); with the majorant
 // fixed, dT/drho_v = sum_i -T/(1 - d_i/rho_max) * w_iv / rho_max.
+template <bool SP>
 __global__ void __launch_bounds__(256)
     k_volume_tr_adj(GridDev G, VRays R, int64_t n, uint64_t seed, const float *__restrict__ dLdT,
                     const float *__restrict__ T, const float *__restrict__ ck_t, const uint32_t *__restrict__ ck_k,
@@ -71,7 +73,7 @@ __global__ void __launch_bounds__(256)
     k = __ldg(ck_k + i);
   } else {
     float cc;
-    ratio_track(G, maj, inv_maj, o, d, tmax, seed, i, t, k, cc);
+    ratio_track<SP>(G, maj, inv_maj, o, d, tmax, seed, i, t, k, cc);
   }
   float t_min, t_max;
   if (!box_pbrt(G, o, d, tmax, t_min, t_max)) return;
@@ -86,14 +88,14 @@ __global__ void __launch_bounds__(256)
     if (t >= t_max) break;
     int x, y, z;
     float fx, fy, fz;
-    float dens = sample_grid(G, o.x + d.x * t, o.y + d.y * t, o.z + d.z * t, x, y, z, fx, fy, fz);
+    float dens = sample_grid<SP>(G, o.x + d.x * t, o.y + d.y * t, o.z + d.z * t, x, y, z, fx, fy, fz);
     float xr = dens * inv_maj;
     if (!(xr > 0.0f)) continue;
     float coef = base / (1.0f - xr);
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
-      const int64_t off = grid_voxel(G, x + cx, y + cy, z + cz);
+      const int64_t off = grid_voxel<SP>(G, x + cx, y + cy, z + cz);
       if (off < 0) continue;  // outside, or an empty brick of a sparse grid (not a parameter)
       float w = (cx ? fx : 1.0f - fx) * (cy ? fy : 1.0f - fy) * (cz ? fz : 1.0f - fz);
       atomicAdd(grad + off, coef * w);
@@ -101,6 +103,7 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+template <bool SP>
 __global__ void __launch_bounds__(256)
     k_volume_sample(GridDev G, VRays R, int64_t n, uint64_t seed, uint8_t *__restrict__ success,
                     float *__restrict__ p, float *__restrict__ weight) {
@@ -113,7 +116,7 @@ __global__ void __launch_bounds__(256)
   RayStream rs;
   rs.init(seed, (uint64_t)i, 0u);
   float3 q = make_float3(0.0f, 0.0f, 0.0f);
-  const uint8_t ok = delta_track(G, maj, o, d, tmax, rs, q) ? 1 : 0;
+  const uint8_t ok = delta_track<SP>(G, maj, o, d, tmax, rs, q) ? 1 : 0;
   const float px = q.x, py = q.y, pz = q.z, w = ok ? G.sigma_s / G.sigma_t : 1.0f;
   success[i] = ok;
   p[3 * i] = px;
@@ -345,10 +348,9 @@ FLG_API int flg_volume_tr(flg_ctx ctx, flg_grid grid, const flg_rays *rays, int6
   if (n > 0 && !T) return set_error(ctx, FLG_ERR_ARG, "T is NULL");
   if (ckpt && (!ckpt->t || !ckpt->k || !ckpt->c)) return set_error(ctx, FLG_ERR_ARG, "checkpoint array is NULL");
   if (n == 0) return FLG_OK;
-  k_volume_tr<<<(unsigned)ceil_div(n, 256), 256, 0, ctx->stream>>>(grid_dev(grid), V, n, seed, T,
-                                                                    ckpt ? ckpt->t : nullptr,
-                                                                    ckpt ? ckpt->k : nullptr,
-                                                                    ckpt ? ckpt->c : nullptr);
+  auto *kern = grid->bidx ? k_volume_tr<true> : k_volume_tr<false>;
+  kern<<<(unsigned)ceil_div(n, 256), 256, 0, ctx->stream>>>(
+      grid_dev(grid), V, n, seed, T, ckpt ? ckpt->t : nullptr, ckpt ? ckpt->k : nullptr, ckpt ? ckpt->c : nullptr);
   FLG_LAUNCH_CHECK(ctx, "k_volume_tr");
   return FLG_OK;
 }
@@ -362,9 +364,9 @@ FLG_API int flg_volume_tr_adjoint(flg_ctx ctx, flg_grid grid, const flg_rays *ra
   if (n > 0 && (!dLdT || !T || !grad)) return set_error(ctx, FLG_ERR_ARG, "NULL argument");
   if (ckpt && (!ckpt->t || !ckpt->k)) return set_error(ctx, FLG_ERR_ARG, "checkpoint array is NULL");
   if (n == 0) return FLG_OK;
-  k_volume_tr_adj<<<(unsigned)ceil_div(n, 256), 256, 0, ctx->stream>>>(grid_dev(grid), V, n, seed, dLdT, T,
-                                                                        ckpt ? ckpt->t : nullptr,
-                                                                        ckpt ? ckpt->k : nullptr, grad);
+  auto *kern = grid->bidx ? k_volume_tr_adj<true> : k_volume_tr_adj<false>;
+  kern<<<(unsigned)ceil_div(n, 256), 256, 0, ctx->stream>>>(
+      grid_dev(grid), V, n, seed, dLdT, T, ckpt ? ckpt->t : nullptr, ckpt ? ckpt->k : nullptr, grad);
   FLG_LAUNCH_CHECK(ctx, "k_volume_tr_adj");
   return FLG_OK;
 }
@@ -377,8 +379,8 @@ FLG_API int flg_volume_sample(flg_ctx ctx, flg_grid grid, const flg_rays *rays, 
   if (rc) return rc;
   if (n > 0 && (!success || !p || !weight)) return set_error(ctx, FLG_ERR_ARG, "NULL output");
   if (n == 0) return FLG_OK;
-  k_volume_sample<<<(unsigned)ceil_div(n, 256), 256, 0, ctx->stream>>>(grid_dev(grid), V, n, seed, success, p,
-                                                                        weight);
+  auto *kern = grid->bidx ? k_volume_sample<true> : k_volume_sample<false>;
+  kern<<<(unsigned)ceil_div(n, 256), 256, 0, ctx->stream>>>(grid_dev(grid), V, n, seed, success, p, weight);
   FLG_LAUNCH_CHECK(ctx, "k_volume_sample");
   return FLG_OK;
 }

@@ -27,22 +27,26 @@ struct GridDev {
 };
 
 // Offset of voxel (x, y, z) in rho, or -1 outside the grid or in an empty
-// brick.
+// brick.  SP selects the sparse lookup at compile time, so the dense kernels
+// keep their plain index arithmetic.
+template <bool SP>
 __device__ __forceinline__ int64_t grid_voxel(const GridDev &G, int x, int y, int z) {
   if (x < 0 || y < 0 || z < 0 || x >= G.nx || y >= G.ny || z >= G.nz) return -1;
-  if (!G.bidx) return ((int64_t)z * G.ny + y) * G.nx + x;
+  if (!SP) return ((int64_t)z * G.ny + y) * G.nx + x;
   const int32_t slot = __ldg(G.bidx + ((int64_t)(z / kBrick) * G.bny + y / kBrick) * G.bnx + x / kBrick);
   if (slot < 0) return -1;
   return (int64_t)slot * (kBrick * kBrick * kBrick) + ((z % kBrick) * kBrick + y % kBrick) * kBrick + x % kBrick;
 }
 
+template <bool SP>
 __device__ __forceinline__ float gat(const GridDev &G, int x, int y, int z) {
-  const int64_t o = grid_voxel(G, x, y, z);
+  const int64_t o = grid_voxel<SP>(G, x, y, z);
   return o < 0 ? 0.0f : __ldg(G.rho + o);
 }
 
 __device__ __forceinline__ float lerpf(float a, float b, float w) { return a + (b - a) * w; }
 
+template <bool SP>
 __device__ __forceinline__ float sample_grid(const GridDev &G, float px, float py, float pz, int &x, int &y, int &z,
                                              float &fx, float &fy, float &fz) {
   float gx = (px - G.lo[0]) * G.scale[0];
@@ -55,10 +59,10 @@ __device__ __forceinline__ float sample_grid(const GridDev &G, float px, float p
   fx = gx - x0;
   fy = gy - y0;
   fz = gz - z0;
-  float c00 = lerpf(gat(G, x, y, z), gat(G, x + 1, y, z), fx);
-  float c10 = lerpf(gat(G, x, y + 1, z), gat(G, x + 1, y + 1, z), fx);
-  float c01 = lerpf(gat(G, x, y, z + 1), gat(G, x + 1, y, z + 1), fx);
-  float c11 = lerpf(gat(G, x, y + 1, z + 1), gat(G, x + 1, y + 1, z + 1), fx);
+  float c00 = lerpf(gat<SP>(G, x, y, z), gat<SP>(G, x + 1, y, z), fx);
+  float c10 = lerpf(gat<SP>(G, x, y + 1, z), gat<SP>(G, x + 1, y + 1, z), fx);
+  float c01 = lerpf(gat<SP>(G, x, y, z + 1), gat<SP>(G, x + 1, y, z + 1), fx);
+  float c11 = lerpf(gat<SP>(G, x, y + 1, z + 1), gat<SP>(G, x + 1, y + 1, z + 1), fx);
   float c0 = lerpf(c00, c10, fy);
   float c1 = lerpf(c01, c11, fy);
   return lerpf(c0, c1, fz);
@@ -87,6 +91,7 @@ __device__ __forceinline__ bool box_pbrt(const GridDev &G, const float3 &o, cons
 
 // Ratio tracking of one ray; returns T and the state after the last
 // roulette survival.
+template <bool SP>
 __device__ __forceinline__ float ratio_track(const GridDev &G, float maj, float inv_maj, const float3 &o,
                                              const float3 &d, float tmax, uint64_t seed, int64_t ray, float &ck_t,
                                              uint32_t &ck_k, float &ck_c) {
@@ -107,7 +112,7 @@ __device__ __forceinline__ float ratio_track(const GridDev &G, float maj, float 
     if (t >= t_max) break;
     int x, y, z;
     float fx, fy, fz;
-    float dens = sample_grid(G, o.x + d.x * t, o.y + d.y * t, o.z + d.z * t, x, y, z, fx, fy, fz);
+    float dens = sample_grid<SP>(G, o.x + d.x * t, o.y + d.y * t, o.z + d.z * t, x, y, z, fx, fy, fz);
     tr *= 1.0f - fmaxf(0.0f, dens * inv_maj);
     if (tr < G.rr) {
       float q = fmaxf(0.05f, 1.0f - tr);
@@ -147,6 +152,7 @@ inline GridDev grid_dev(flg_grid g) {
 // Delta tracking of one ray over [0, tmax] (volume.cpp:109-148): true on a
 // real collision, with its position in p.  Draws from rs: one uniform per
 // step plus one for the collision test.
+template <bool SP>
 __device__ __forceinline__ bool delta_track(const GridDev &G, float maj, const float3 &o, const float3 &d,
                                             float tmax, RayStream &rs, float3 &p) {
   float t_min, t_max;
@@ -161,7 +167,7 @@ __device__ __forceinline__ bool delta_track(const GridDev &G, float maj, const f
     float qx = o.x + d.x * t, qy = o.y + d.y * t, qz = o.z + d.z * t;
     int x, y, z;
     float fx, fy, fz;
-    float dens = sample_grid(G, qx, qy, qz, x, y, z, fx, fy, fz);
+    float dens = sample_grid<SP>(G, qx, qy, qz, x, y, z, fx, fy, fz);
     float p_s = G.sigma_s * dens / max_mu;
     float p_a = G.sigma_a * dens / max_mu;
     float p_n = 1.0f - p_s - p_a;
