@@ -141,15 +141,24 @@ def _trace_opts(stack_depth=0, block_threads=0, persistent=0, refill_lanes=0, ra
     return FlgTraceOpts(stack_depth, block_threads, persistent, refill_lanes, ray_sort)
 
 
+def _builder_id(name: str) -> int:
+    """'lbvh' (the Karras radix tree) or 'ploc' (locally-ordered clustering)."""
+    ids = {"lbvh": _lib.FLG_BUILDER_LBVH, "ploc": _lib.FLG_BUILDER_PLOC}
+    if name not in ids:
+        raise ValueError(f"builder must be one of {sorted(ids)}")
+    return ids[name]
+
+
 class RadixBVHBuilder:
     """GPU Karras LBVH with the BVHBuilderBase interface (base_bvh.hpp:105-117)."""
 
     def __init__(self, mesh: InternalTriangleMesh, ctx: Optional[Context] = None, node_width: int = 4,
-                 leaf_size: int = 1):
+                 leaf_size: int = 1, builder: str = "lbvh"):
         self.mesh = mesh
         self.ctx = ctx or Context(mesh.p.device.index or 0)
         self.node_width = node_width
         self.leaf_size = leaf_size
+        self.builder = _builder_id(builder)
         self.h = None
 
     def build(self) -> None:
@@ -158,7 +167,7 @@ class RadixBVHBuilder:
             self.ctx.check(lib.flg_bvh_rebuild(self.ctx.h, self.h, C.c_void_p(_ptr(self.mesh.p))))
             return
         h = C.c_void_p()
-        opts = FlgBuildOpts(self.node_width, self.leaf_size, 1)
+        opts = FlgBuildOpts(self.node_width, self.leaf_size, 1, self.builder)
         self.ctx.check(lib.flg_bvh_build(self.ctx.h, C.c_void_p(_ptr(self.mesh.p)),
                                          C.c_void_p(_ptr(self.mesh.ind)), self.mesh.n_tri,
                                          self.mesh.n_vert, C.byref(opts), C.byref(h)))
@@ -227,8 +236,8 @@ class BatchedRadixBVHBuilder(RadixBVHBuilder):
     """Many scenes built in one segmented launch and traced in one launch."""
 
     def __init__(self, mesh: InternalTriangleMesh, tri_offsets: Sequence[int], ctx: Optional[Context] = None,
-                 node_width: int = 4, leaf_size: int = 1):
-        super().__init__(mesh, ctx, node_width, leaf_size)
+                 node_width: int = 4, leaf_size: int = 1, builder: str = "lbvh"):
+        super().__init__(mesh, ctx, node_width, leaf_size, builder)
         self.tri_offsets = np.ascontiguousarray(np.asarray(tri_offsets, dtype=np.int64))
 
     def build(self) -> None:
@@ -237,7 +246,7 @@ class BatchedRadixBVHBuilder(RadixBVHBuilder):
             self.ctx.check(lib.flg_bvh_rebuild(self.ctx.h, self.h, C.c_void_p(_ptr(self.mesh.p))))
             return
         h = C.c_void_p()
-        opts = FlgBuildOpts(self.node_width, self.leaf_size, 1)
+        opts = FlgBuildOpts(self.node_width, self.leaf_size, 1, self.builder)
         offs = self.tri_offsets.ctypes.data_as(C.POINTER(C.c_int64))
         self.ctx.check(lib.flg_bvh_build_batched(self.ctx.h, C.c_void_p(_ptr(self.mesh.p)),
                                                  C.c_void_p(_ptr(self.mesh.ind)), offs,

@@ -27,7 +27,11 @@ class FlgHits(C.Structure):
 
 
 class FlgBuildOpts(C.Structure):
-    _fields_ = [("node_width", C.c_int32), ("leaf_size", C.c_int32), ("keep_topology", C.c_int32)]
+    _fields_ = [("node_width", C.c_int32), ("leaf_size", C.c_int32), ("keep_topology", C.c_int32),
+                ("builder", C.c_int32)]
+
+
+FLG_BUILDER_LBVH, FLG_BUILDER_PLOC = 0, 1
 
 
 class FlgTraceOpts(C.Structure):

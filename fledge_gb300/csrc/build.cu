@@ -40,34 +40,6 @@ __device__ __forceinline__ void atomic_max_f(float *a, float v) {
   else atomicMin((unsigned int *)a, __float_as_uint(v));
 }
 
-__device__ __forceinline__ void tri_verts(const float *__restrict__ pos, const int32_t *__restrict__ idx,
-                                          int64_t t, float3 &a, float3 &b, float3 &c) {
-  int64_t i0, i1, i2;
-  if (idx) {
-    i0 = idx[3 * t];
-    i1 = idx[3 * t + 1];
-    i2 = idx[3 * t + 2];
-  } else {
-    i0 = 3 * t;
-    i1 = 3 * t + 1;
-    i2 = 3 * t + 2;
-  }
-  a = make_float3(pos[3 * i0], pos[3 * i0 + 1], pos[3 * i0 + 2]);
-  b = make_float3(pos[3 * i1], pos[3 * i1 + 1], pos[3 * i1 + 2]);
-  c = make_float3(pos[3 * i2], pos[3 * i2 + 1], pos[3 * i2 + 2]);
-}
-
-// BVHBuilderBase::Triangle::getBound (base_bvh.hpp:90-102): std::min/max
-// order; fminf/fmaxf agree on finite input up to the sign of zero.
-__device__ __forceinline__ void tri_box(float3 a, float3 b, float3 c, float *lo, float *hi) {
-  lo[0] = fminf(fminf(a.x, b.x), c.x);
-  lo[1] = fminf(fminf(a.y, b.y), c.y);
-  lo[2] = fminf(fminf(a.z, b.z), c.z);
-  hi[0] = fmaxf(fmaxf(a.x, b.x), c.x);
-  hi[1] = fmaxf(fmaxf(a.y, b.y), c.y);
-  hi[2] = fmaxf(fmaxf(a.z, b.z), c.z);
-}
-
 __global__ void k_init_boxes(float *box, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
@@ -404,8 +376,6 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
   FLG_CUDA(ctx, cudaMemsetAsync(b->d_lookback, 0,
                                 sizeof(uint32_t) * 256 * (size_t)b->n_tiles * b->n_passes, st));
   FLG_CUDA(ctx, cudaMemsetAsync(b->d_tile_ctr, 0, sizeof(uint32_t) * b->n_passes, st));
-  if (b->n_nodes > 0) {
-  }
 
   k_scene_bounds<<<grid_for(n, kBoundsChunk), kBoundsThreads, 0, st>>>(b->pos, b->idx, n, b->d_tri_off,
                                                                      b->n_scenes, b->d_scene_box);
@@ -417,6 +387,12 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
   FLG_LAUNCH_CHECK(ctx, "k_morton_hist");
   int rc = sort_enqueue(ctx, b);
   if (rc) return rc;
+  if (b->builder == FLG_BUILDER_PLOC) {
+    rc = ploc_build(ctx, b);
+    if (rc) return rc;
+    if (b->width > 2) return collapse_enqueue(ctx, b, b->width, b->leaf_size);
+    return FLG_OK;
+  }
   if (b->n_nodes > 0) {
     k_karras<<<grid_for(b->n_nodes, 256, (int64_t)ctx->num_sms * 16), 256, 0, st>>>(
         b->d_keys, b->d_tri_off, b->d_node_off, b->n_scenes, b->n_nodes, b->d_split, b->d_leaf,
@@ -459,6 +435,9 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   int leaf_size = opts && opts->leaf_size ? opts->leaf_size : 1;
   if (width != 2 && width != 4 && width != 8) return set_error(ctx, FLG_ERR_ARG, "node_width must be 2, 4 or 8");
   if (leaf_size < 1 || leaf_size > 8) return set_error(ctx, FLG_ERR_ARG, "leaf_size must be in [1, 8]");
+  const int builder = opts ? opts->builder : FLG_BUILDER_LBVH;
+  if (builder != FLG_BUILDER_LBVH && builder != FLG_BUILDER_PLOC)
+    return set_error(ctx, FLG_ERR_ARG, "builder must be FLG_BUILDER_LBVH or FLG_BUILDER_PLOC");
 
   flg_bvh b = new flg_bvh_t();
   b->ctx = ctx;
@@ -470,6 +449,7 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   b->width = width;
   b->leaf_size = leaf_size;
   b->keep_topology = opts ? opts->keep_topology != 0 : true;
+  b->builder = builder;
   b->tri_off_h.assign(tri_off_host, tri_off_host + n_scenes + 1);
   b->node_off_h.resize(n_scenes + 1);
   b->node_off_h[0] = 0;
@@ -480,6 +460,7 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
     root[s] = c >= 2 ? (int32_t)b->node_off_h[s] : c == 1 ? ~(int32_t)tri_off_host[s] : INT32_MIN;
   }
   b->n_nodes = b->node_off_h[n_scenes];
+  for (int s = 0; s < n_scenes; ++s) b->n_nonempty += tri_off_host[s + 1] > tri_off_host[s] ? 1 : 0;
   b->n_morton_passes = 4;
   int scene_passes = 0;
   if (n_scenes > 1) scene_passes = n_scenes <= 256 ? 1 : n_scenes <= 65536 ? 2 : 3;
@@ -510,6 +491,7 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   A(&b->d_hist, 3 * 256 * (size_t)b->n_passes);
   A(&b->d_lookback, 256 * (size_t)b->n_tiles * b->n_passes);
   A(&b->d_tile_ctr, b->n_passes);
+  if (rc == FLG_OK && builder == FLG_BUILDER_PLOC) rc = ploc_reserve(b);
   if (rc) {
     flg_bvh_destroy(b);
     return rc;
@@ -614,6 +596,8 @@ FLG_API int flg_bvh_info_get(flg_bvh bvh, flg_bvh_info *out) {
 FLG_API int flg_bvh_download(flg_bvh bvh, int32_t scene, flg_bvh_topology *t) {
   if (!bvh || !t) return FLG_ERR_ARG;
   flg_ctx ctx = bvh->ctx;
+  if (bvh->builder != FLG_BUILDER_LBVH)
+    return set_error(ctx, FLG_ERR_UNSUPPORTED, "only LBVH handles keep the Karras arrays");
   if (scene < 0 || scene >= bvh->n_scenes) return set_error(ctx, FLG_ERR_ARG, "scene out of range");
   cudaStream_t st = ctx->stream;
   const int64_t toff = bvh->tri_off_h[scene], noff = bvh->node_off_h[scene];

@@ -27,7 +27,13 @@ __device__ __forceinline__ float half_area(const Cand &c) {
   return dx * dy + dy * dz + dz * dx;
 }
 
-__device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, const int32_t *__restrict__ range_j,
+// Leaf ranges of internal nodes: from the Karras range ends (range_j) or,
+// for PLOC trees, from the explicit depth-first ranges (rfirst / rcount).
+struct Ranges {
+  const int32_t *range_j, *rfirst, *rcount;
+};
+
+__device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, const Ranges &R,
                                             const int64_t *__restrict__ tri_off,
                                             const int64_t *__restrict__ node_off, int32_t ref, Cand &c0,
                                             Cand &c1) {
@@ -47,11 +53,14 @@ __device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, co
     if (r[k] < 0) {
       c.first = ~r[k];
       c.count = 1;
+    } else if (R.rfirst) {
+      c.first = R.rfirst[r[k]];
+      c.count = R.rcount[r[k]];
     } else {
       const Node2 &cn = nodes2[r[k]];
       int s = cn.d.w;
       int li = (int)(r[k] - node_off[s]);
-      int j = range_j[r[k]];
+      int j = R.range_j[r[k]];
       c.first = (int32_t)tri_off[s] + min(li, j);
       c.count = abs(li - j) + 1;
     }
@@ -64,7 +73,7 @@ __device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, co
 // serialised in L2.
 template <int W>
 __global__ void __launch_bounds__(128)
-    k_collapse_level(const Node2 *__restrict__ nodes2, const int32_t *__restrict__ range_j,
+    k_collapse_level(const Node2 *__restrict__ nodes2, Ranges R,
                      const int64_t *__restrict__ tri_off, const int64_t *__restrict__ node_off, int leaf_size,
                      const int2 *__restrict__ q_in, const int32_t *__restrict__ q_in_count, int2 *__restrict__ q_out,
                      int32_t *q_out_count, int32_t *node_ctr, int64_t cap, NodeW<W> *__restrict__ wide,
@@ -86,7 +95,7 @@ __global__ void __launch_bounds__(128)
         atomicOr(err, kErrQueue);  // a hole left by an overflowing level
       } else {
         nc = 2;
-        child_cands(nodes2, range_j, tri_off, node_off, item.x, c[0], c[1]);
+        child_cands(nodes2, R, tri_off, node_off, item.x, c[0], c[1]);
       }
     }
     while (nc >= 2 && nc < W) {
@@ -108,7 +117,7 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
       for (int k = 0; k < W; ++k)
         if (k == best) r = c[k].ref;
-      child_cands(nodes2, range_j, tri_off, node_off, r, a, b);
+      child_cands(nodes2, R, tri_off, node_off, r, a, b);
 #pragma unroll
       for (int k = 0; k < W; ++k) {
         if (k == best) c[k] = a;
@@ -240,7 +249,8 @@ static int collapse_levels(flg_ctx ctx, flg_bvh b) {
   // levels (millions of items in large batches), early exit on small ones.
   const unsigned grid = (unsigned)ctx->num_sms * 32;
   for (int L = 0; L < kMaxLevels; ++L) {
-    k_collapse_level<W><<<grid, 128, 0, st>>>(b->d_nodes2, b->d_range_j, b->d_tri_off, b->d_node_off,
+    k_collapse_level<W><<<grid, 128, 0, st>>>(b->d_nodes2, Ranges{b->d_range_j, b->d_rfirst, b->d_rcount},
+                                              b->d_tri_off, b->d_node_off,
                                               b->leaf_size, b->d_queue[L & 1], b->d_wide_ctr + 1 + L,
                                               b->d_queue[(L + 1) & 1], b->d_wide_ctr + 2 + L, b->d_wide_ctr,
                                               b->wide_cap, wide, ctx->d_err);

@@ -343,4 +343,33 @@ __device__ __forceinline__ int find_segment(const int64_t *off, int n_seg, int64
   return lo;
 }
 
+// Vertices of triangle t of a soup (idx NULL) or an indexed mesh.
+__device__ __forceinline__ void tri_verts(const float *__restrict__ pos, const int32_t *__restrict__ idx,
+                                          int64_t t, float3 &a, float3 &b, float3 &c) {
+  int64_t i0, i1, i2;
+  if (idx) {
+    i0 = idx[3 * t];
+    i1 = idx[3 * t + 1];
+    i2 = idx[3 * t + 2];
+  } else {
+    i0 = 3 * t;
+    i1 = 3 * t + 1;
+    i2 = 3 * t + 2;
+  }
+  a = make_float3(pos[3 * i0], pos[3 * i0 + 1], pos[3 * i0 + 2]);
+  b = make_float3(pos[3 * i1], pos[3 * i1 + 1], pos[3 * i1 + 2]);
+  c = make_float3(pos[3 * i2], pos[3 * i2 + 1], pos[3 * i2 + 2]);
+}
+
+// BVHBuilderBase::Triangle::getBound (base_bvh.hpp:90-102): std::min/max
+// order; fminf/fmaxf agree on finite input up to the sign of zero.
+__device__ __forceinline__ void tri_box(float3 a, float3 b, float3 c, float *lo, float *hi) {
+  lo[0] = fminf(fminf(a.x, b.x), c.x);
+  lo[1] = fminf(fminf(a.y, b.y), c.y);
+  lo[2] = fminf(fminf(a.z, b.z), c.z);
+  hi[0] = fmaxf(fmaxf(a.x, b.x), c.x);
+  hi[1] = fmaxf(fmaxf(a.y, b.y), c.y);
+  hi[2] = fmaxf(fmaxf(a.z, b.z), c.z);
+}
+
 }  // namespace flg

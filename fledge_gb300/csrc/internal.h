@@ -120,6 +120,17 @@ struct flg_bvh_t {
   std::vector<void *> allocs;
   int64_t device_bytes = 0;
   bool keep_topology = true;
+  // PLOC builds (builder == FLG_BUILDER_PLOC): the leaf range of every BVH2
+  // node in the final (depth-first) triangle order, used by the collapse, and
+  // the clustering scratch (ping-pong cluster arrays, scan buffers, queues).
+  int32_t builder = 0;
+  int32_t *d_rfirst = nullptr, *d_rcount = nullptr;
+  float4 *d_cbox[2] = {nullptr, nullptr};  // 2 per cluster: lo, hi
+  int32_t *d_cref[2] = {nullptr, nullptr}, *d_ccnt[2] = {nullptr, nullptr}, *d_cscene[2] = {nullptr, nullptr};
+  int32_t *d_nn = nullptr, *d_valid = nullptr, *d_pos = nullptr, *d_bsum = nullptr, *d_mctr = nullptr;
+  int32_t *d_newpos = nullptr, *d_lcount = nullptr;
+  int2 *d_lq[2] = {nullptr, nullptr};
+  int32_t n_nonempty = 0;
 };
 
 struct flg_grid_t {
@@ -190,6 +201,8 @@ int build_enqueue(flg_ctx ctx, flg_bvh b);
 int collapse_reserve(flg_ctx ctx, flg_bvh b);
 int collapse_enqueue(flg_ctx ctx, flg_bvh b, int width, int leaf_size);
 int sort_enqueue(flg_ctx ctx, flg_bvh b);
+int ploc_reserve(flg_bvh b);
+int ploc_build(flg_ctx ctx, flg_bvh b);
 int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_rays *rays, int64_t n,
                   const flg_trace_opts *opts, const int64_t *ray_off_dev, int n_scenes, flg_hits *hits,
                   uint8_t *occ);

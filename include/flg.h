@@ -75,7 +75,18 @@ typedef struct flg_build_opts {
   int32_t node_width;     /* traversal layout: 2, 4 or 8 (0 = 4) */
   int32_t leaf_size;      /* wide layouts: max triangles per leaf range (0 = 1) */
   int32_t keep_topology;  /* keep the Karras arrays for flg_bvh_download */
+  int32_t builder;        /* FLG_BUILDER_LBVH (0, the Karras radix tree) or FLG_BUILDER_PLOC */
 } flg_build_opts;
+
+/* Tree builders.  FLG_BUILDER_PLOC is the high-quality alternative to the
+ * LBVH (the role of BasicBVHBuilder's SAH build, src/experimental/
+ * base_bvh.cpp:33-188): parallel locally-ordered clustering over the same
+ * Morton order (Meister & Bittner 2018), i.e. repeated merging of mutual
+ * nearest clusters within a window of the sorted sequence, by the surface
+ * area of the merged box.  Its builds synchronise with the host once per
+ * clustering iteration (not capturable), and its handles keep no Karras
+ * arrays (flg_bvh_download returns FLG_ERR_UNSUPPORTED). */
+enum { FLG_BUILDER_LBVH = 0, FLG_BUILDER_PLOC = 1 };
 
 typedef struct flg_trace_opts {
   int32_t stack_depth;    /* 32 or 64 (0 = 64); overflowing rays are retried deeper */

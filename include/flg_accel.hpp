@@ -73,8 +73,10 @@ struct DeviceMesh {
 
 class RadixBVHBuilder {
  public:
-  RadixBVHBuilder(Context &ctx, const DeviceMesh &mesh, int node_width = 4, int leaf_size = 1)
-      : ctx_(ctx), mesh_(mesh), opts_{node_width, leaf_size, 1} {}
+  // builder: FLG_BUILDER_LBVH (the Karras radix tree) or FLG_BUILDER_PLOC.
+  RadixBVHBuilder(Context &ctx, const DeviceMesh &mesh, int node_width = 4, int leaf_size = 1,
+                  int builder = FLG_BUILDER_LBVH)
+      : ctx_(ctx), mesh_(mesh), opts_{node_width, leaf_size, 1, builder} {}
   ~RadixBVHBuilder() { flg_bvh_destroy(h_); }
   RadixBVHBuilder(const RadixBVHBuilder &) = delete;
   RadixBVHBuilder &operator=(const RadixBVHBuilder &) = delete;
