@@ -38,9 +38,15 @@ __device__ __forceinline__ int64_t grid_voxel(const GridDev &G, int x, int y, in
   return (int64_t)slot * (kBrick * kBrick * kBrick) + ((z % kBrick) * kBrick + y % kBrick) * kBrick + x % kBrick;
 }
 
+// Density at lattice point (x, y, z), background 0 outside.  The dense path
+// tests the bounds before forming the index (as a plain branch around the
+// load): routing it through grid_voxel's -1 sentinel cost 25 % of the
+// tracking throughput.
 template <bool SP>
 __device__ __forceinline__ float gat(const GridDev &G, int x, int y, int z) {
-  const int64_t o = grid_voxel<SP>(G, x, y, z);
+  if (x < 0 || y < 0 || z < 0 || x >= G.nx || y >= G.ny || z >= G.nz) return 0.0f;
+  if (!SP) return __ldg(G.rho + ((int64_t)z * G.ny + y) * G.nx + x);
+  const int64_t o = grid_voxel<true>(G, x, y, z);
   return o < 0 ? 0.0f : __ldg(G.rho + o);
 }
 
