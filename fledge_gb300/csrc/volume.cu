@@ -95,8 +95,13 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
       const int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
-      const int64_t off = grid_voxel<SP>(G, x + cx, y + cy, z + cz);
-      if (off < 0) continue;  // outside, or an empty brick of a sparse grid (not a parameter)
+      const int X = x + cx, Y = y + cy, Z = z + cz;
+      if (X < 0 || Y < 0 || Z < 0 || X >= G.nx || Y >= G.ny || Z >= G.nz) continue;
+      int64_t off = ((int64_t)Z * G.ny + Y) * G.nx + X;
+      if (SP) {
+        off = grid_voxel<true>(G, X, Y, Z);
+        if (off < 0) continue;  // an empty brick of a sparse grid is not a parameter
+      }
       float w = (cx ? fx : 1.0f - fx) * (cy ? fy : 1.0f - fy) * (cz ? fz : 1.0f - fz);
       atomicAdd(grad + off, coef * w);
     }
