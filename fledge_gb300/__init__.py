@@ -137,8 +137,10 @@ def _alloc_hits(n: int, device):
             "v": torch.empty(n, dtype=torch.float32, device=device)}
 
 
-def _trace_opts(stack_depth=0, block_threads=0, persistent=0, refill_lanes=0, ray_sort=0) -> FlgTraceOpts:
-    return FlgTraceOpts(stack_depth, block_threads, persistent, refill_lanes, ray_sort)
+def _trace_opts(stack_depth=0, block_threads=0, persistent=0, refill_lanes=0, ray_sort=0,
+                tri_test=0) -> FlgTraceOpts:
+    """tri_test: 0 watertight Pluecker, 1 the live renderer's Moller-Trumbore."""
+    return FlgTraceOpts(stack_depth, block_threads, persistent, refill_lanes, ray_sort, tri_test)
 
 
 def _builder_id(name: str) -> int:

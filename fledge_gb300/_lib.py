@@ -36,7 +36,7 @@ FLG_BUILDER_LBVH, FLG_BUILDER_PLOC = 0, 1
 
 class FlgTraceOpts(C.Structure):
     _fields_ = [("stack_depth", C.c_int32), ("block_threads", C.c_int32), ("persistent", C.c_int32),
-                ("refill_lanes", C.c_int32), ("ray_sort", C.c_int32)]
+                ("refill_lanes", C.c_int32), ("ray_sort", C.c_int32), ("tri_test", C.c_int32)]
 
 
 class FlgBvhInfo(C.Structure):

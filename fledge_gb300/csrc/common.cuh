@@ -200,6 +200,30 @@ __device__ __forceinline__ bool pluecker_core(float3 a, float3 b, float3 c, floa
   return true;
 }
 
+// Triangle::intersect of the live renderer (shape.cpp:100-148): Moller-
+// Trumbore, not watertight; zero-area triangles never hit (area() == 0);
+// accepts 0 < t, the caller applies t < tMax.  Same operation order as the
+// reference (its Dot/Cross/Norm, vector.h:364-404).
+__device__ __forceinline__ bool moller_t(float3 p0, float3 p1, float3 p2, float3 O, float3 D, float &t) {
+  const float3 e1 = f3sub(p1, p0), e2 = f3sub(p2, p0);
+  const float3 n = f3cross(e1, e2);
+  if (sqrtf(f3dot(n, n)) / 2.0f == 0.0f) return false;
+  const float3 p = f3cross(D, e2);
+  const float d = f3dot(e1, p);
+  const float inv_det = __frcp_rn(d);
+  if (d == 0.0f) return false;
+  const float3 tv = f3sub(O, p0);
+  const float u = f3dot(tv, p) * inv_det;
+  if (u < 0.0f || u > 1.0f) return false;
+  const float3 q = f3cross(tv, e1);
+  const float v = f3dot(D, q) * inv_det;
+  if (v < 0.0f || u + v > 1.0f) return false;
+  const float tn = f3dot(e2, q) * inv_det;
+  if (!(tn > 0.0f)) return false;
+  t = tn;
+  return true;
+}
+
 // The traversal's test: t only (the closest hit's barycentrics are formed
 // once, for the winner).
 __device__ __forceinline__ bool pluecker_t(float3 a, float3 b, float3 c, float3 O, float3 D, float &t) {

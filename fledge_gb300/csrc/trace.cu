@@ -64,28 +64,38 @@ __device__ __forceinline__ int32_t scene_root(const int32_t *__restrict__ roots,
 }
 
 // Tests sorted triangle g; updates the closest hit.  Returns true on accept.
+// MT selects the live renderer's Moller-Trumbore test and its strict
+// t < tMax rule instead of the watertight Pluecker test.
+template <bool MT = false>
 __device__ __forceinline__ bool test_tri(const TriRec *__restrict__ tris, int64_t g, const float3 &o,
                                          const float3 &d, float tmin, float &best, bool &have, int32_t &prim) {
   const float4 *p = (const float4 *)(tris + g);
   float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
   float t;
-  if (!pluecker_t(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z), o, d, t))
-    return false;
-  if (!accept_closest(t, tmin, best, have)) return false;
+  const float3 pa = make_float3(a.x, a.y, a.z), pb = make_float3(b.x, b.y, b.z), pc = make_float3(c.x, c.y, c.z);
+  if (MT) {
+    if (!moller_t(pa, pb, pc, o, d, t)) return false;
+    if (!(t >= tmin && t < best)) return false;
+  } else {
+    if (!pluecker_t(pa, pb, pc, o, d, t)) return false;
+    if (!accept_closest(t, tmin, best, have)) return false;
+  }
   best = t;
   have = true;
   prim = (int32_t)g;  // sorted position; write_result maps it to the original id
   return true;
 }
 
-// Any-hit variant: accepts t in [tmin, tmax].
+// Any-hit variant: accepts t in [tmin, tmax] ([tmin, tmax) with MT).
+template <bool MT = false>
 __device__ __forceinline__ bool test_tri_any(const TriRec *__restrict__ tris, int64_t g, const float3 &o,
                                              const float3 &d, float tmin, float tmax) {
   const float4 *p = (const float4 *)(tris + g);
   float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
   float t;
-  if (!pluecker_t(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), make_float3(c.x, c.y, c.z), o, d, t))
-    return false;
+  const float3 pa = make_float3(a.x, a.y, a.z), pb = make_float3(b.x, b.y, b.z), pc = make_float3(c.x, c.y, c.z);
+  if (MT) return moller_t(pa, pb, pc, o, d, t) && t >= tmin && t < tmax;
+  if (!pluecker_t(pa, pb, pc, o, d, t)) return false;
   return t >= tmin && !(t > tmax);
 }
 
@@ -130,7 +140,7 @@ __device__ __forceinline__ void record_overflow(const Scratch &S, int64_t ray) {
 // ----------------------------------------------------------------------------
 // BVH2 traversal (reference-faithful leaf handling).
 // ----------------------------------------------------------------------------
-template <bool ANY, int STACK>
+template <bool ANY, int STACK, bool MT = false>
 __device__ __forceinline__ bool trace_bvh2(const Node2 *__restrict__ nodes, const TriRec *__restrict__ tris,
                                            int32_t root, const float3 &o, const float3 &d, const float3 &inv,
                                            float tmin, float tmax, bool &have, int32_t &prim, float &best) {
@@ -139,8 +149,8 @@ __device__ __forceinline__ bool trace_bvh2(const Node2 *__restrict__ nodes, cons
   prim = -1;
   if (root == INT32_MIN) return true;
   if (root < 0) {
-    if (ANY) have = test_tri_any(tris, ~(int64_t)root, o, d, tmin, tmax);
-    else test_tri(tris, ~(int64_t)root, o, d, tmin, best, have, prim);
+    if (ANY) have = test_tri_any<MT>(tris, ~(int64_t)root, o, d, tmin, tmax);
+    else test_tri<MT>(tris, ~(int64_t)root, o, d, tmin, best, have, prim);
     return true;
   }
   uint64_t stk[STACK];
@@ -154,16 +164,16 @@ __device__ __forceinline__ bool trace_bvh2(const Node2 *__restrict__ nodes, cons
     const int32_t c0 = Dd.x, c1 = Dd.y;
     if (c0 < 0) {
       if (ANY) {
-        if (test_tri_any(tris, ~(int64_t)c0, o, d, tmin, tmax)) { have = true; return true; }
+        if (test_tri_any<MT>(tris, ~(int64_t)c0, o, d, tmin, tmax)) { have = true; return true; }
       } else {
-        test_tri(tris, ~(int64_t)c0, o, d, tmin, best, have, prim);
+        test_tri<MT>(tris, ~(int64_t)c0, o, d, tmin, best, have, prim);
       }
     }
     if (c1 < 0) {
       if (ANY) {
-        if (test_tri_any(tris, ~(int64_t)c1, o, d, tmin, tmax)) { have = true; return true; }
+        if (test_tri_any<MT>(tris, ~(int64_t)c1, o, d, tmin, tmax)) { have = true; return true; }
       } else {
-        test_tri(tris, ~(int64_t)c1, o, d, tmin, best, have, prim);
+        test_tri<MT>(tris, ~(int64_t)c1, o, d, tmin, best, have, prim);
       }
     }
     const float lim = ANY ? tmax : best;
@@ -191,7 +201,7 @@ __device__ __forceinline__ bool trace_bvh2(const Node2 *__restrict__ nodes, cons
   }
 }
 
-template <bool ANY>
+template <bool ANY, bool MT = false>
 __global__ void __launch_bounds__(256)
     k_trace_bvh2(const Node2 *__restrict__ nodes, const TriRec *__restrict__ tris, const int32_t *__restrict__ roots,
                  const int64_t *__restrict__ ray_off, int n_scenes, RaySoA R, int64_t n, Out O, Scratch S) {
@@ -204,7 +214,7 @@ __global__ void __launch_bounds__(256)
   bool have;
   int32_t prim;
   float best;
-  if (!trace_bvh2<ANY, 64>(nodes, tris, root, o, d, inv, tmin, tmax, have, prim, best)) {
+  if (!trace_bvh2<ANY, 64, MT>(nodes, tris, root, o, d, inv, tmin, tmax, have, prim, best)) {
     record_overflow(S, i);
     return;
   }
@@ -433,7 +443,7 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-template <int W, bool ANY>
+template <int W, bool ANY, bool MT = false>
 __global__ void __launch_bounds__(128)
     k_trace_retry(const NodeW<(W == 2 ? 4 : W)> *__restrict__ nodes, const Node2 *__restrict__ nodes2,
                   const TriRec *__restrict__ tris,
@@ -450,7 +460,7 @@ __global__ void __launch_bounds__(128)
       bool have;
       int32_t prim;
       float best;
-      if (!trace_bvh2<ANY, kRetryStack>(nodes2, tris, root, o, d, inv, tmin, tmax, have, prim, best)) {
+      if (!trace_bvh2<ANY, kRetryStack, MT>(nodes2, tris, root, o, d, inv, tmin, tmax, have, prim, best)) {
         atomicOr(S.err, kErrStack);
         continue;
       }
@@ -719,6 +729,7 @@ int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_ra
   if (op.block_threads != 64 && op.block_threads != 128 && op.block_threads != 256)
     return set_error(ctx, FLG_ERR_ARG, "block_threads must be 64, 128 or 256");
   if (op.ray_sort) return set_error(ctx, FLG_ERR_UNSUPPORTED, "ray_sort is not implemented");
+  if (op.tri_test != 0 && op.tri_test != 1) return set_error(ctx, FLG_ERR_ARG, "tri_test must be 0 or 1");
   int rc = ensure_trace_scratch(ctx);
   if (rc) return rc;
   if (n == 0) return FLG_OK;
@@ -730,6 +741,27 @@ int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_ra
   FLG_CUDA(ctx, cudaMemsetAsync(S.ovf_count, 0, sizeof(uint32_t), st));
   FLG_CUDA(ctx, cudaMemsetAsync(S.work, 0, sizeof(unsigned long long), st));
   const bool any = occ != nullptr;
+  if (op.tri_test == 1) {
+    // The live renderer's Moller-Trumbore test: one ray per thread over the
+    // BVH2 layout (kept by every handle), overflow retried with a deep stack.
+    const unsigned g = (unsigned)ceil_div(n, 256);
+    if (any)
+      k_trace_bvh2<true, true><<<g, 256, 0, st>>>(b->d_nodes2, b->d_tris, b->d_root, ray_off_dev, n_scenes, R, n, O,
+                                                  S);
+    else
+      k_trace_bvh2<false, true><<<g, 256, 0, st>>>(b->d_nodes2, b->d_tris, b->d_root, ray_off_dev, n_scenes, R, n, O,
+                                                   S);
+    FLG_LAUNCH_CHECK(ctx, "trace kernel");
+    const unsigned rg = (unsigned)ctx->num_sms;
+    if (any)
+      k_trace_retry<2, true, true><<<rg, 128, 0, st>>>(nullptr, b->d_nodes2, b->d_tris, b->d_root, ray_off_dev,
+                                                       n_scenes, R, O, S);
+    else
+      k_trace_retry<2, false, true><<<rg, 128, 0, st>>>(nullptr, b->d_nodes2, b->d_tris, b->d_root, ray_off_dev,
+                                                        n_scenes, R, O, S);
+    FLG_LAUNCH_CHECK(ctx, "trace retry kernel");
+    return FLG_OK;
+  }
   if (b->width == 2) {
     const unsigned g = (unsigned)ceil_div(n, 256);
     if (any)

@@ -96,6 +96,10 @@ typedef struct flg_trace_opts {
                              postponing (wide layouts) */
   int32_t refill_lanes;   /* persistent: refill a warp once this many lanes idle (0 = 16) */
   int32_t ray_sort;       /* 0: none; 1: sort rays by direction octant and origin cell */
+  int32_t tri_test;       /* 0: watertight Pluecker (intersector.hpp:63-101, the experimental
+                             path); 1: the live renderer's Moller-Trumbore Triangle::intersect
+                             (shape.cpp:100-148; hits need 0 < t < tmax), traced one ray per
+                             thread over the BVH2 layout */
 } flg_trace_opts;
 
 /* ------------------------------- context -------------------------------- */

@@ -220,7 +220,7 @@ struct Karras {
 // u = U/(U+V+W), v = V/(U+V+W) (Embree's barycentric convention; the reference
 // computes U, V, W but returns no barycentrics).
 // ---------------------------------------------------------------------------
-enum { MODE_REF = 0, MODE_DEFECT = 1, MODE_DEV = 2 };
+enum { MODE_REF = 0, MODE_DEFECT = 1, MODE_DEV = 2, MODE_MT = 3 };
 
 struct V3 { float x, y, z; };
 inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
@@ -244,7 +244,33 @@ inline V3 stable_triangle_normal(V3 a, V3 b, V3 c) {
 
 struct Hit { float t, u, v; };
 
+// Triangle::intersect of the live renderer (shape.cpp:100-148): Moller-
+// Trumbore, not watertight; degenerate (zero-area) triangles never hit;
+// accepts 0 < t (the caller applies t < tMax).
+inline bool moller(V3 p0, V3 p1, V3 p2, V3 O, V3 D, Hit *h) {
+  const V3 e1 = sub(p1, p0), e2 = sub(p2, p0);
+  const V3 n = cross(e1, e2);
+  if (std::sqrt(dot(n, n)) / 2.0f == 0.0f) return false;  // area() == 0
+  const V3 p = cross(D, e2);
+  const float d = dot(e1, p);
+  const float inv_det = 1.0f / d;
+  if (d == 0.0f) return false;
+  const V3 t = sub(O, p0);
+  const float u = dot(t, p) * inv_det;
+  if (u < 0.0f || u > 1.0f) return false;
+  const V3 q = cross(t, e1);
+  const float v = dot(D, q) * inv_det;
+  if (v < 0.0f || u + v > 1.0f) return false;
+  const float tn = dot(e2, q) * inv_det;
+  if (!(tn > 0.0f)) return false;
+  h->t = tn;
+  h->u = u;
+  h->v = v;
+  return true;
+}
+
 inline bool pluecker(V3 a, V3 b, V3 c, V3 O, V3 D, int mode, Hit *h) {
+  if (mode == MODE_MT) return moller(a, b, c, O, D, h);
   V3 v0 = sub(a, O), v1 = sub(b, O), v2 = sub(c, O);
   V3 e0 = sub(v2, v0), e1 = sub(v0, v1), e2 = sub(v1, v2);
   float U = dot(cross(e0, add(v2, v0)), D);
@@ -432,6 +458,7 @@ void recursive_intersect(const Tree &T, const Mesh &M, int node, const RayIn &r,
     Hit h;
     if (!pluecker(ld3(M.v(tri, 0)), ld3(M.v(tri, 1)), ld3(M.v(tri, 2)), O, D, mode, &h)) continue;
     if (h.t > b.tfar) continue;
+    if (mode == MODE_MT && !(h.t < b.tfar)) continue;  // the live renderer rejects t >= tMax
     if (h.t < r.tmin) continue;
     b.tfar = h.t;
     b.prim = tri;
@@ -458,7 +485,7 @@ bool recursive_occluded(const Tree &T, const Mesh &M, int node, const RayIn &r, 
     int tri = T.perm[s + side];
     Hit h;
     if (!pluecker(ld3(M.v(tri, 0)), ld3(M.v(tri, 1)), ld3(M.v(tri, 2)), O, D, mode, &h)) continue;
-    if (h.t > r.tmax || h.t < r.tmin) continue;
+    if (h.t > r.tmax || h.t < r.tmin || (mode == MODE_MT && !(h.t < r.tmax))) continue;
     return true;
   }
   if (!(lf & 1) && recursive_occluded(T, M, s, r, mode)) return true;
@@ -805,12 +832,12 @@ ORC_API void orc_trace_closest(const float *pos, const int32_t *idx, int64_t n_t
     if (n_tri == 1) {
       Hit h;
       if (pluecker(ld3(M.v(0, 0)), ld3(M.v(0, 1)), ld3(M.v(0, 2)), ld3(r.o), ld3(r.d), mode, &h) &&
-          !(h.t > b.tfar) && !(h.t < r.tmin))
+          !(h.t > b.tfar) && !(mode == MODE_MT && !(h.t < b.tfar)) && !(h.t < r.tmin))
         b = Best{h.t, 0, h.u, h.v};
     } else if (n_tri > 1) {
       recursive_intersect(T, M, 0, r, mode, b);
     }
-    if (mode == MODE_DEV && b.prim >= 0) {
+    if ((mode == MODE_DEV || mode == MODE_MT) && b.prim >= 0) {
       // The GPU reports the selected triangle's t, u, v recomputed in
       // float-float arithmetic and rounded once; same operations here.
       refine_tuv(M.v(b.prim, 0), M.v(b.prim, 1), M.v(b.prim, 2), r.o, r.d, b.tfar, b.u, b.v);
@@ -834,7 +861,7 @@ ORC_API void orc_trace_any(const float *pos, const int32_t *idx, int64_t n_tri, 
     if (n_tri == 1) {
       Hit h;
       occ = pluecker(ld3(M.v(0, 0)), ld3(M.v(0, 1)), ld3(M.v(0, 2)), ld3(r.o), ld3(r.d), mode, &h) &&
-            !(h.t > r.tmax) && !(h.t < r.tmin);
+            !(h.t > r.tmax) && !(h.t < r.tmin) && !(mode == MODE_MT && !(h.t < r.tmax));
     } else if (n_tri > 1) {
       occ = recursive_occluded(T, M, 0, r, mode);
     }

@@ -15,7 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 
-MODE_REF, MODE_DEFECT, MODE_DEV = 0, 1, 2
+MODE_REF, MODE_DEFECT, MODE_DEV, MODE_MT = 0, 1, 2, 3
 
 _lib = None
 

@@ -199,3 +199,29 @@ def test_autotune_runs_and_keeps_parity(ctx, oracle, c0_case):
                             persistent=best.persistent, refill_lanes=best.refill_lanes))
     bad, _, _ = U.compare_closest(oracle, pos, None, tree, r8, hg, oracle.MODE_DEV)
     assert bad == 0
+
+
+@pytest.mark.parametrize("w", [2, 4])
+def test_moller_trumbore_mode_matches_oracle(ctx, oracle, c0_case, w):
+    """tri_test=1: the live renderer's Moller-Trumbore Triangle::intersect
+    (shape.cpp:100-148) with its strict t < tMax rule, over the BVH2 layout of
+    any handle; closest hits and occlusion as the oracle's MT mode (ids equal
+    except recorded exact ties, t/u/v equal where the ids agree)."""
+    pos, r8, tree = c0_case
+    b, _ = U.gpu_build(ctx, pos, width=w)
+    rd, _ = U.rays_dev(r8)
+    hg = U.host(b.intersect(rd, tri_test=1))
+    ctx.sync()
+    bad, ties, ho = U.compare_closest(oracle, pos, None, tree, r8, hg, oracle.MODE_MT)
+    assert bad == 0, f"{bad} prim mismatches ({ties} exact ties)"
+    same = hg["prim"] == ho["prim"]
+    for k in ("t", "u", "v"):
+        assert np.array_equal(hg[k][same], ho[k][same]), k
+    assert (hg["prim"] >= 0).mean() > 0.3
+    short = r8.copy()
+    short[7] = np.random.default_rng(6).uniform(1.0, 2.5, r8.shape[1]).astype(np.float32)
+    rs, _ = U.rays_dev(short)
+    occ = b.intersectP(rs, tri_test=1).cpu().numpy()
+    ref = oracle.trace_any(pos, None, tree, short, oracle.MODE_MT)
+    assert np.array_equal(occ, ref), np.count_nonzero(occ != ref)
+

@@ -152,6 +152,23 @@ def test_pluecker_exact(oracle):
         assert not oracle.pluecker(a, b, c, [0.25, 0.25, 1.0], [0, 0, 1], mode)[0]  # behind
 
 
+def test_moller_trumbore_known_answers(oracle):
+    """The live renderer's Triangle::intersect (shape.cpp:100-148) as restated
+    in the oracle: exact hits, barycentrics (u on p1, v on p2), and the cases
+    it rejects — zero area, parallel rays, hits behind the origin, outside the
+    triangle."""
+    a, b, c = (0, 0, 0), (1, 0, 0), (0, 1, 0)
+    ok, h = oracle.pluecker(a, b, c, (0.25, 0.5, 1.0), (0, 0, -1), oracle.MODE_MT)
+    assert ok and h[0] == 1.0 and h[1] == 0.25 and h[2] == 0.5
+    assert not oracle.pluecker(a, b, (2, 0, 0), (0.25, 0.0, 1.0), (0, 0, -1), oracle.MODE_MT)[0]  # area 0
+    assert not oracle.pluecker(a, b, c, (0.25, 0.25, 1.0), (1, 0, 0), oracle.MODE_MT)[0]  # parallel
+    assert not oracle.pluecker(a, b, c, (0.25, 0.25, -1.0), (0, 0, -1), oracle.MODE_MT)[0]  # behind
+    assert not oracle.pluecker(a, b, c, (0.75, 0.75, 1.0), (0, 0, -1), oracle.MODE_MT)[0]  # u + v > 1
+    # a hit on the watertight test's side agrees on t and barycentrics with it
+    okp, hp = oracle.pluecker(a, b, c, (0.25, 0.5, 1.0), (0, 0, -1), oracle.MODE_REF)
+    assert okp and np.allclose(hp, h)
+
+
 def test_reference_normalize_defect(oracle):
     # common/vector.h:495-503 sums z instead of z*z: a normal with a large
     # negative z gives sqrt(negative) = NaN and the reference misses.
