@@ -109,6 +109,7 @@ FLG_API int flg_ctx_destroy(flg_ctx c) {
   cudaFree(c->d_ray_off);
   cudaFree(c->stage);
   cudaFree(c->pt_buf);
+  cudaFree(c->rs_buf);
   delete c;
   return FLG_OK;
 }

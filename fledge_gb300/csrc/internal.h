@@ -76,6 +76,9 @@ struct flg_ctx_t {
   // Wavefront queues of flg_pathtrace (grown on demand).
   void *pt_buf = nullptr;
   size_t pt_bytes = 0;
+  // Ray-sort scratch of trace_enqueue (grown on demand).
+  void *rs_buf = nullptr;
+  size_t rs_bytes = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
@@ -201,6 +204,9 @@ int build_enqueue(flg_ctx ctx, flg_bvh b);
 int collapse_reserve(flg_ctx ctx, flg_bvh b);
 int collapse_enqueue(flg_ctx ctx, flg_bvh b, int width, int leaf_size);
 int sort_enqueue(flg_ctx ctx, flg_bvh b);
+int64_t sort_tiles(int64_t n);
+int sort_pairs_enqueue(flg_ctx ctx, cudaStream_t st, int64_t n, int passes, uint32_t *const keys[2],
+                       uint32_t *const vals[2], uint32_t *hist, uint32_t *lookback, uint32_t *tile_ctr);
 int ploc_reserve(flg_bvh b);
 int ploc_build(flg_ctx ctx, flg_bvh b);
 int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_rays *rays, int64_t n,

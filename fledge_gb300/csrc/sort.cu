@@ -205,4 +205,32 @@ int sort_enqueue(flg_ctx ctx, flg_bvh b) {
   return FLG_OK;
 }
 
+// Generic (key, index) sort used by the ray sort: keys[0] holds n keys and
+// hist[0 .. passes) their per-pass digit counts; the sorted keys and the
+// original indices end in keys[passes & 1] / vals[passes & 1].  hist needs
+// 2 * passes * 256 words, lookback passes * tiles * 256, tile_ctr passes.
+int sort_pairs_enqueue(flg_ctx ctx, cudaStream_t st, int64_t n, int passes, uint32_t *const keys[2],
+                       uint32_t *const vals[2], uint32_t *hist, uint32_t *lookback, uint32_t *tile_ctr) {
+  if (n <= 0) return FLG_OK;
+  const int64_t tiles = sort_tiles(n);
+  uint32_t *off = hist + (size_t)passes * kRadix;
+  FLG_CUDA(ctx, cudaMemsetAsync(lookback, 0, sizeof(uint32_t) * kRadix * (size_t)tiles * passes, st));
+  FLG_CUDA(ctx, cudaMemsetAsync(tile_ctr, 0, sizeof(uint32_t) * passes, st));
+  k_scan_hist<<<passes, kRadix, 0, st>>>(hist, off);
+  FLG_LAUNCH_CHECK(ctx, "k_scan_hist");
+  for (int p = 0; p < passes; ++p) {
+    uint32_t *lb = lookback + (size_t)p * tiles * kRadix;
+    if (p == 0)
+      k_onesweep<true><<<(unsigned)tiles, kSortThreads, 0, st>>>(keys[0], nullptr, keys[1], vals[1], n, 0, 0, nullptr,
+                                                                  1, off, lb, tile_ctr, ctx->d_err, ctx->spin_limit);
+    else
+      k_onesweep<false><<<(unsigned)tiles, kSortThreads, 0, st>>>(keys[p & 1], vals[p & 1], keys[(p + 1) & 1],
+                                                                   vals[(p + 1) & 1], n, 8 * p, 0, nullptr, 1,
+                                                                   off + (size_t)p * kRadix, lb, tile_ctr + p,
+                                                                   ctx->d_err, ctx->spin_limit);
+    FLG_LAUNCH_CHECK(ctx, "k_onesweep");
+  }
+  return FLG_OK;
+}
+
 }  // namespace flg

@@ -481,6 +481,82 @@ __global__ void __launch_bounds__(128)
 // Host side.
 // ----------------------------------------------------------------------------
 
+// ----------------------------------------------------------------------------
+// Ray sort (flg_trace_opts.ray_sort = 1): rays of a single-scene trace are
+// reordered by a 30-bit key — direction octant (3 bits) above a 27-bit Morton
+// code of the origin in the scene box enlarged by its extent on every side —
+// traced in that order, and their hits written back in the caller's order.
+// Neighbouring lanes then start in the same region heading the same way.
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    k_ray_keys(RaySoA R, int64_t n, const float *__restrict__ box, uint32_t *__restrict__ keys,
+               uint32_t *__restrict__ hist) {
+  __shared__ uint32_t s_hist[4][256];
+  for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0u;
+  __syncthreads();
+  float lo[3], sc[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float e = box[3 + k] - box[k];
+    lo[k] = box[k] - e;
+    sc[k] = e > 0.0f ? 1.0f / (3.0f * e) : 0.0f;
+  }
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float o[3] = {__ldg(R.ox + i), __ldg(R.oy + i), __ldg(R.oz + i)};
+    const float d[3] = {__ldg(R.dx + i), __ldg(R.dy + i), __ldg(R.dz + i)};
+    uint32_t q[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float u = fminf(fmaxf((o[k] - lo[k]) * sc[k], 0.0f), 1.0f);
+      q[k] = min((uint32_t)(u * 512.0f), 511u);  // NaN origins land in cell 0
+    }
+    const uint32_t oct = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+    const uint32_t key = (oct << 27) | (left_shift3(q[2]) << 2) | (left_shift3(q[1]) << 1) | left_shift3(q[0]);
+    keys[i] = key;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) atomicAdd(&s_hist[p][(key >> (8 * p)) & 0xFFu], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) {
+    const uint32_t c = (&s_hist[0][0])[i];
+    if (c) atomicAdd(&hist[i], c);
+  }
+}
+
+// Sorted position j takes ray perm[j].
+__global__ void k_ray_gather(RaySoA R, int64_t n, const uint32_t *__restrict__ perm, float *__restrict__ out) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = perm[j];
+    if (i < 0 || i >= n) continue;  // only a timed-out sort leaves such slots (error word set)
+    out[j] = __ldg(R.ox + i);
+    out[n + j] = __ldg(R.oy + i);
+    out[2 * n + j] = __ldg(R.oz + i);
+    out[3 * n + j] = __ldg(R.dx + i);
+    out[4 * n + j] = __ldg(R.dy + i);
+    out[5 * n + j] = __ldg(R.dz + i);
+    out[6 * n + j] = R.tmin ? __ldg(R.tmin + i) : R.tmin_c;
+    out[7 * n + j] = R.tmax ? __ldg(R.tmax + i) : R.tmax_c;
+  }
+}
+
+// Hits of sorted position j go back to ray perm[j].
+__global__ void k_ray_scatter(int64_t n, const uint32_t *__restrict__ perm, const int32_t *__restrict__ prim,
+                              const float *__restrict__ t, const float *__restrict__ u, const float *__restrict__ v,
+                              const uint8_t *__restrict__ occ, Out O) {
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = perm[j];
+    if (i < 0 || i >= n) continue;
+    if (occ) {
+      O.occ[i] = occ[j];
+    } else {
+      O.prim[i] = prim[j];
+      O.t[i] = t[j];
+      O.u[i] = u[j];
+      O.v[i] = v[j];
+    }
+  }
+}
+
 static int ensure_trace_scratch(flg_ctx ctx) {
   if (ctx->d_ovf) return FLG_OK;
   if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "first trace allocates; not allowed during capture");
@@ -728,13 +804,66 @@ int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_ra
   if (op.stack_depth != 32 && op.stack_depth != 64) return set_error(ctx, FLG_ERR_ARG, "stack_depth must be 32 or 64");
   if (op.block_threads != 64 && op.block_threads != 128 && op.block_threads != 256)
     return set_error(ctx, FLG_ERR_ARG, "block_threads must be 64, 128 or 256");
-  if (op.ray_sort) return set_error(ctx, FLG_ERR_UNSUPPORTED, "ray_sort is not implemented");
+  if (op.ray_sort != 0 && op.ray_sort != 1) return set_error(ctx, FLG_ERR_ARG, "ray_sort must be 0 or 1");
+  if (op.ray_sort && (ray_off_dev || n_scenes != 1))
+    return set_error(ctx, FLG_ERR_UNSUPPORTED, "ray_sort applies to single-scene traces");
+  if (op.ray_sort && n > ((int64_t)1 << 28)) return set_error(ctx, FLG_ERR_UNSUPPORTED, "ray_sort: at most 2^28 rays");
   if (op.tri_test != 0 && op.tri_test != 1) return set_error(ctx, FLG_ERR_ARG, "tri_test must be 0 or 1");
   int rc = ensure_trace_scratch(ctx);
   if (rc) return rc;
   if (n == 0) return FLG_OK;
   RaySoA R{rays->ox, rays->oy, rays->oz, rays->dx, rays->dy, rays->dz, rays->tmin, rays->tmax,
            rays->tmin_const, rays->tmax_const};
+  if (op.ray_sort) {
+    // Scratch: keys and indices (2 x 2), digit counts and offsets, look-back,
+    // tile counters, the sorted rays (8 arrays) and their hits (4 arrays).
+    const int64_t tiles = sort_tiles(n);
+    const size_t w = (size_t)n * 4;
+    const size_t need = 4 * w + 2 * 4 * 256 * 4 + (size_t)4 * tiles * 256 * 4 + 64 + 8 * w + 4 * w + 16 * 256;
+    if (ctx->rs_bytes < need) {
+      if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "ray-sort scratch grows; not allowed during capture");
+      cudaFree(ctx->rs_buf);
+      ctx->rs_buf = nullptr;
+      ctx->rs_bytes = 0;
+      FLG_CUDA(ctx, cudaMalloc(&ctx->rs_buf, need));
+      ctx->rs_bytes = need;
+    }
+    char *bp = (char *)ctx->rs_buf;
+    auto take = [&](size_t bytes) {
+      char *p = bp;
+      bp += (bytes + 255) & ~(size_t)255;
+      return (void *)p;
+    };
+    uint32_t *keys[2] = {(uint32_t *)take(w), (uint32_t *)take(w)};
+    uint32_t *vals[2] = {(uint32_t *)take(w), (uint32_t *)take(w)};
+    uint32_t *hist = (uint32_t *)take(2 * 4 * 256 * 4);
+    uint32_t *lookback = (uint32_t *)take((size_t)4 * tiles * 256 * 4);
+    uint32_t *tile_ctr = (uint32_t *)take(64);
+    float *sr = (float *)take(8 * w);
+    float *sh = (float *)take(4 * w);
+    if (bp > (char *)ctx->rs_buf + need) return set_error(ctx, FLG_ERR_STATE, "ray-sort buffer layout");
+    FLG_CUDA(ctx, cudaMemsetAsync(hist, 0, sizeof(uint32_t) * 4 * 256, st));
+    const unsigned g = grid_for(n, 256, (int64_t)ctx->num_sms * 8);
+    k_ray_keys<<<g, 256, 0, st>>>(R, n, b->d_scene_box, keys[0], hist);
+    FLG_LAUNCH_CHECK(ctx, "k_ray_keys");
+    rc = sort_pairs_enqueue(ctx, st, n, 4, keys, vals, hist, lookback, tile_ctr);
+    if (rc) return rc;
+    const uint32_t *perm = vals[0];  // 4 passes: the result is back in buffer 0
+    k_ray_gather<<<g, 256, 0, st>>>(R, n, perm, sr);
+    FLG_LAUNCH_CHECK(ctx, "k_ray_gather");
+    flg_rays sorted{sr, sr + n, sr + 2 * n, sr + 3 * n, sr + 4 * n, sr + 5 * n, sr + 6 * n, sr + 7 * n, 0.0f, 0.0f};
+    flg_trace_opts op2 = op;
+    op2.ray_sort = 0;
+    uint8_t *socc = occ ? (uint8_t *)sh : nullptr;
+    flg_hits shits{(int32_t *)sh, sh + n, sh + 2 * n, sh + 3 * n};
+    rc = trace_enqueue(ctx, st, set, b, &sorted, n, &op2, nullptr, 1, occ ? nullptr : &shits, socc);
+    if (rc) return rc;
+    Out O{hits ? hits->prim : nullptr, hits ? hits->t : nullptr, hits ? hits->u : nullptr,
+          hits ? hits->v : nullptr, occ};
+    k_ray_scatter<<<g, 256, 0, st>>>(n, perm, (const int32_t *)sh, sh + n, sh + 2 * n, sh + 3 * n, socc, O);
+    FLG_LAUNCH_CHECK(ctx, "k_ray_scatter");
+    return FLG_OK;
+  }
   Out O{hits ? hits->prim : nullptr, hits ? hits->t : nullptr, hits ? hits->u : nullptr,
         hits ? hits->v : nullptr, occ};
   Scratch S = scratch_for(ctx, set);

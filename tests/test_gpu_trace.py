@@ -225,3 +225,32 @@ def test_moller_trumbore_mode_matches_oracle(ctx, oracle, c0_case, w):
     ref = oracle.trace_any(pos, None, tree, short, oracle.MODE_MT)
     assert np.array_equal(occ, ref), np.count_nonzero(occ != ref)
 
+
+
+@pytest.mark.parametrize("w,opts", [(2, {}), (4, {"persistent": 2, "refill_lanes": 8}), (8, {"persistent": 1})])
+def test_ray_sort_gives_identical_hits(ctx, c0_case, w, opts):
+    """ray_sort=1 traces the rays in octant / origin-Morton order and writes
+    the hits back in the caller's order: every ray's result is the same as
+    without sorting (closest and any hit)."""
+    pos, r8, _ = c0_case
+    b, _ = U.gpu_build(ctx, pos, width=w)
+    rd, _ = U.rays_dev(r8)
+    h0 = U.host(b.intersect(rd, **opts))
+    h1 = U.host(b.intersect(rd, ray_sort=1, **opts))
+    for k in ("prim", "t", "u", "v"):
+        assert np.array_equal(h0[k], h1[k]), k
+    o0 = b.intersectP(rd, **opts).cpu().numpy()
+    o1 = b.intersectP(rd, ray_sort=1, **opts).cpu().numpy()
+    assert np.array_equal(o0, o1)
+    ctx.sync()
+
+
+def test_ray_sort_rejects_batched_traces(ctx):
+    import fledge_gb300 as F
+    offs = np.array([0, 100, 300], np.int64)
+    pos = F.gen_triangles(ctx, 300, 3)
+    soa = F.gen_rays(ctx, 300 * 4, 4)
+    bb = F.BatchedRadixBVHBuilder(F.InternalTriangleMesh(pos), offs, ctx, node_width=4)
+    bb.build()
+    with pytest.raises(F.FlgError):
+        bb.intersect_batched(F.Rays.from_soa(soa), offs * 4, ray_sort=1)
