@@ -1115,11 +1115,34 @@ FLG_API int flg_autotune_trace(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, i
   {
     int best_leaf = bl;
     rc = flg_bvh_set_width(ctx, bvh, bw, best_leaf);
-    char tail[256];
+    if (rc) goto done;
+    // The ray-sort key, tried on the best layout: it pays when neighbouring
+    // rays are scattered, costs a sort and two gathers when they are not.
+    flg_trace_opts op = bo;
+    op.ray_sort = 1;
+    rc = trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, &op, nullptr, 1, &h, nullptr);
+    if (rc) goto done;
+    cudaEventRecord(e0, ctx->stream);
+    for (int r = 0; r < 3 && !rc; ++r) rc = trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, &op, nullptr, 1, &h, nullptr);
+    if (rc) goto done;
+    cudaEventRecord(e1, ctx->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms /= 3.0f;
+    char line[160];
+    snprintf(line, sizeof(line), ", {\"ray_sort\": 1, \"on_best\": true, \"ms\": %.5f, \"mrays_s\": %.2f}", ms,
+             n / (ms * 1e3));
+    rec += line;
+    if (ms < best_ms) {
+      best_ms = ms;
+      bo = op;
+    }
+    char tail[288];
     snprintf(tail, sizeof(tail),
              "], \"best\": {\"node_width\": %d, \"leaf_size\": %d, \"stack_depth\": %d, \"persistent\": %d, "
-             "\"refill_lanes\": %d, \"block_threads\": %d, \"ms\": %.5f}}",
-             bw, best_leaf, bo.stack_depth, bo.persistent, bo.refill_lanes, bo.block_threads, best_ms);
+             "\"refill_lanes\": %d, \"block_threads\": %d, \"ray_sort\": %d, \"ms\": %.5f}}",
+             bw, best_leaf, bo.stack_depth, bo.persistent, bo.refill_lanes, bo.block_threads, bo.ray_sort, best_ms);
     rec += tail;
   }
 done:
