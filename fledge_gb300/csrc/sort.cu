@@ -4,8 +4,9 @@
 // tbb::parallel_sort of 32-byte RadixTriangle records (radix_bvh.cpp:77-81);
 // the sort is stable, so equal codes keep ascending original index.
 //
-// One launch per 8-bit digit.  Each CTA claims a tile of 4096 pairs in launch
-// order, ranks its keys with warp match-any, publishes its per-digit counts,
+// One launch per 8-bit digit.  Each CTA claims a tile of 3072 pairs (256
+// threads x 12) in launch order, ranks its keys with warp match-any and
+// shared-memory atomics, publishes its per-digit counts,
 // resolves its global offsets by looking back over earlier tiles, reorders
 // the tile in shared memory and writes runs of equal digits contiguously.
 // Batched builds append passes whose digit is the scene of the pair (from
@@ -17,9 +18,11 @@ namespace flg {
 
 constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortItems = 16;
+constexpr int kSortItems = 12;  // 12 x 4 CTAs per SM beat 8 / 16 items and 2 / 3 CTAs
+constexpr int kSortMinBlocks = 4;  // CTAs per SM the register budget allows
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kRadix = 256;
+constexpr int kLookback = 4;  // predecessor tiles read per look-back step
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kFlagMask = 3u << 30;
@@ -27,25 +30,38 @@ constexpr uint32_t kValMask = (1u << 30) - 1u;
 
 __device__ __forceinline__ void st_volatile(uint32_t *p, uint32_t v) { *(volatile uint32_t *)p = v; }
 
-__device__ __forceinline__ uint32_t sort_digit(uint32_t key, uint32_t val, int shift, int scene_mode,
-                                               const int64_t *tri_off, int n_scenes) {
-  if (!scene_mode) return (key >> shift) & 0xFFu;
-  uint32_t s = (uint32_t)find_segment(tri_off, n_scenes, (int64_t)val);
+// Digit of a pair in this pass: a byte of the key, or (scene passes) a byte
+// of the scene that the pair's triangle index falls in.
+template <bool kScene>
+__device__ __forceinline__ uint32_t sort_digit(uint32_t key, uint32_t val, int shift, const int64_t *tri_off,
+                                               int n_scenes) {
+  if (!kScene) return (key >> shift) & 0xFFu;
+  const uint32_t s = (uint32_t)find_segment(tri_off, n_scenes, (int64_t)val);
   return (s >> shift) & 0xFFu;
 }
 
-template <bool kFirst>
-__global__ void __launch_bounds__(kSortThreads)
+// One pass over one tile.  Phases: (1) each warp loads 32 x kSortItems
+// consecutive pairs (coalesced, no bounds checks on full tiles); (2) ranks
+// them: per item, the lanes holding the same digit find each other with
+// match-any and their lowest lane adds the group's size to the warp's
+// counter for that digit with a shared-memory atomic whose old value is the
+// group's base.  The atomics of successive items of a warp are issued back
+// to back (nothing waits for the previous item's counter), and a warp's
+// shared-memory operations are performed in issue order, so ranks follow
+// item order and the sort stays stable; (3) column scan of the warp counters
+// (warp offsets) and scan over digits (tile start), folded into one offset
+// per (warp, digit); (4) publish the tile's counts and look back for the
+// global offsets; (5) scatter the pairs into shared memory in digit order
+// (one 8-byte store each) and write them out in runs of equal digits.
+template <bool kFirst, bool kScene>
+__global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
     k_onesweep(const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int64_t n, int shift,
-               int scene_mode, const int64_t *__restrict__ tri_off, int n_scenes,
-               const uint32_t *__restrict__ pass_off, uint32_t *lookback, uint32_t *tile_ctr,
-               uint32_t *err, uint32_t spin_limit) {
-  __shared__ uint32_t s_keys[kSortTile];
-  __shared__ uint32_t s_vals[kSortTile];
-  __shared__ uint8_t s_dig[kSortTile];
+               const int64_t *__restrict__ tri_off, int n_scenes, const uint32_t *__restrict__ pass_off,
+               uint32_t *lookback, uint32_t *tile_ctr, uint32_t *err, uint32_t spin_limit) {
+  __shared__ uint2 s_kv[kSortTile];
+  __shared__ uint8_t s_dig[kScene ? kSortTile : 1];
   __shared__ uint32_t s_whist[kSortWarps][kRadix];
-  __shared__ uint32_t s_tile_start[kRadix];
   __shared__ int32_t s_glob[kRadix];
   __shared__ uint32_t s_wsum[kSortWarps];
   __shared__ uint32_t s_tile;
@@ -56,29 +72,34 @@ __global__ void __launch_bounds__(kSortThreads)
   __syncthreads();
   const int64_t tile = s_tile;
   const int64_t base = tile * kSortTile;
-  const int64_t wbase = base + (int64_t)warp * (kSortItems * 32);
+  const bool full = base + kSortTile <= n;
+  const int64_t wbase = base + (int64_t)warp * (kSortItems * 32) + lane;
+  // Pairs of this lane left in the input, as a 32-bit bound for the checks.
+  const int64_t wrem64 = n - wbase;
+  const int wrem = wrem64 > kSortTile ? kSortTile : (wrem64 < 0 ? 0 : (int)wrem64);
+  const uint32_t *kin = keys_in + wbase;
+  const uint32_t *vin = kFirst ? nullptr : vals_in + wbase;
 
-  uint32_t k[kSortItems], v[kSortItems], dg[kSortItems], rank[kSortItems];
+  uint32_t k[kSortItems], v[kSortItems], rank[kSortItems];
+  uint32_t dg[kScene ? kSortItems : 1];
 #pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
-    int64_t idx = wbase + j * 32 + lane;
-    bool valid = idx < n;
-    k[j] = valid ? keys_in[idx] : 0xFFFFFFFFu;
-    v[j] = valid ? (kFirst ? (uint32_t)idx : vals_in[idx]) : 0u;
+    const bool valid = full || j * 32 < wrem;
+    k[j] = valid ? kin[j * 32] : 0xFFFFFFFFu;
+    v[j] = valid ? (kFirst ? (uint32_t)wbase + (uint32_t)(j * 32) : vin[j * 32]) : 0u;
   }
   const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
-    int64_t idx = wbase + j * 32 + lane;
-    bool valid = idx < n;
-    uint32_t d = valid ? sort_digit(k[j], v[j], shift, scene_mode, tri_off, n_scenes) : 256u;
-    dg[j] = d;
-    uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
-    uint32_t cnt = valid ? s_whist[warp][d] : 0u;
-    __syncwarp();
-    rank[j] = cnt + __popc(peers & lt);
-    if (valid && (peers & lt) == 0u) s_whist[warp][d] = cnt + __popc(peers);
-    __syncwarp();
+    const bool valid = full || j * 32 < wrem;
+    const uint32_t d = valid ? sort_digit<kScene>(k[j], v[j], shift, tri_off, n_scenes) : 256u;
+    if (kScene) dg[kScene ? j : 0] = d;
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+    const int leader = __ffs(peers) - 1;
+    uint32_t gbase = 0u;
+    if (lane == leader && d < 256u) gbase = atomicAdd(&s_whist[warp][d], (uint32_t)__popc(peers));
+    gbase = __shfl_sync(0xFFFFFFFFu, gbase, leader);
+    rank[j] = gbase + __popc(peers & lt);
   }
   __syncthreads();
 
@@ -94,7 +115,8 @@ __global__ void __launch_bounds__(kSortThreads)
   uint32_t *lb = lookback + (size_t)tile * kRadix;
   st_volatile(lb + d, tile_count | (tile == 0 ? kFlagPrefix : kFlagAgg));
 
-  // Exclusive scan of the tile counts over digits (shared-memory reorder).
+  // Exclusive scan of the tile counts over digits: the digit's start in the
+  // tile's shared-memory reorder, added to every warp's offset.
   uint32_t x = tile_count;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -108,19 +130,38 @@ __global__ void __launch_bounds__(kSortThreads)
   for (int w = 0; w < kSortWarps; ++w)
     if (w < warp) wpre += s_wsum[w];
   const uint32_t tstart = wpre + x - tile_count;
-  s_tile_start[d] = tstart;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) s_whist[w][d] += tstart;
 
-  // Decoupled look-back over earlier tiles.  Each wait is bounded: on a
-  // timeout the error word is set and a (wrong) prefix is still published so
-  // later tiles do not wait on this one; writes stay bounds-checked.
+  // Decoupled look-back over earlier tiles, kLookback predecessors per step:
+  // their flags are read with independent loads, so a walk over m tiles that
+  // have only published aggregates costs m / kLookback L2 round trips instead
+  // of m.  A word read early stays usable (an aggregate never changes; only
+  // its flag may since have become a prefix); an unpublished one is waited
+  // on.  Tile 0 always holds a prefix, so the walk ends there at the latest.
+  // Each wait is bounded: on a timeout the error word is set and a (wrong)
+  // prefix is still published so later tiles do not wait on this one;
+  // writes stay bounds-checked.
   uint32_t excl = 0;
   if (tile > 0) {
     int64_t p = tile - 1;
-    while (p >= 0) {
-      uint32_t s = wait_flag(lookback + (size_t)p * kRadix + d, kFlagMask, spin_limit, err);
-      excl += s & kValMask;
-      if (s == 0u || (s & kFlagPrefix)) break;
-      --p;
+    bool done = false;
+    while (!done) {
+      uint32_t s[kLookback];
+#pragma unroll
+      for (int i = 0; i < kLookback; ++i)
+        s[i] = p - i >= 0 ? ld_volatile(lookback + (size_t)(p - i) * kRadix + d) : 0u;
+#pragma unroll
+      for (int i = 0; i < kLookback; ++i) {
+        if (!done && p - i >= 0) {
+          uint32_t w = s[i];
+          if (!(w & kFlagMask)) w = wait_flag(lookback + (size_t)(p - i) * kRadix + d, kFlagMask, spin_limit, err);
+          excl += w & kValMask;
+          if (w == 0u || (w & kFlagPrefix)) done = true;
+        }
+      }
+      p -= kLookback;
+      if (p < 0) done = true;
     }
     st_volatile(lb + d, ((excl + tile_count) & kValMask) | kFlagPrefix);
   }
@@ -129,23 +170,44 @@ __global__ void __launch_bounds__(kSortThreads)
 
 #pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
-    if (dg[j] < 256u) {
-      uint32_t pos = s_tile_start[dg[j]] + s_whist[warp][dg[j]] + rank[j];
-      s_keys[pos] = k[j];
-      s_vals[pos] = v[j];
-      s_dig[pos] = (uint8_t)dg[j];
+    const uint32_t dj = kScene ? dg[kScene ? j : 0] : ((k[j] >> shift) & 0xFFu);
+    if (full || j * 32 < wrem) {
+      const uint32_t pos = s_whist[warp][dj] + rank[j];
+      s_kv[pos] = make_uint2(k[j], v[j]);
+      if (kScene) s_dig[kScene ? pos : 0] = (uint8_t)dj;
     }
   }
   __syncthreads();
-  int64_t rem = n - base;
+  const int64_t rem = n - base;
   const int tile_valid = rem < kSortTile ? (int)rem : kSortTile;
   for (int i = tid; i < tile_valid; i += kSortThreads) {
-    int64_t out = (int64_t)s_glob[s_dig[i]] + i;
+    const uint2 kv = s_kv[i];
+    const uint32_t di = kScene ? (uint32_t)s_dig[kScene ? i : 0] : ((kv.x >> shift) & 0xFFu);
+    const int64_t out = (int64_t)s_glob[di] + i;
     if (out >= 0 && out < n) {
-      keys_out[out] = s_keys[i];
-      vals_out[out] = s_vals[i];
+      keys_out[out] = kv.x;
+      vals_out[out] = kv.y;
     }
   }
+}
+
+// Launches one pass (the template pair for first / scene passes).
+static void launch_pass(cudaStream_t st, unsigned grid, bool first, bool scene, const uint32_t *in_k,
+                        const uint32_t *in_v, uint32_t *out_k, uint32_t *out_v, int64_t n, int shift,
+                        const int64_t *tri_off, int n_scenes, const uint32_t *pass_off, uint32_t *lb,
+                        uint32_t *tile_ctr, uint32_t *err, uint32_t spin_limit) {
+  if (first && scene)
+    k_onesweep<true, true><<<grid, kSortThreads, 0, st>>>(in_k, in_v, out_k, out_v, n, shift, tri_off, n_scenes,
+                                                          pass_off, lb, tile_ctr, err, spin_limit);
+  else if (first)
+    k_onesweep<true, false><<<grid, kSortThreads, 0, st>>>(in_k, in_v, out_k, out_v, n, shift, tri_off, n_scenes,
+                                                           pass_off, lb, tile_ctr, err, spin_limit);
+  else if (scene)
+    k_onesweep<false, true><<<grid, kSortThreads, 0, st>>>(in_k, in_v, out_k, out_v, n, shift, tri_off, n_scenes,
+                                                           pass_off, lb, tile_ctr, err, spin_limit);
+  else
+    k_onesweep<false, false><<<grid, kSortThreads, 0, st>>>(in_k, in_v, out_k, out_v, n, shift, tri_off, n_scenes,
+                                                            pass_off, lb, tile_ctr, err, spin_limit);
 }
 
 // Exclusive scan of each pass's 256 digit counts (one block per pass).
@@ -191,15 +253,8 @@ int sort_enqueue(flg_ctx ctx, flg_bvh b) {
     uint32_t *lb = b->d_lookback + (size_t)p * b->n_tiles * kRadix;
     uint32_t *in_k = kb[p & 1], *out_k = kb[(p + 1) & 1];
     uint32_t *in_v = vb[p & 1], *out_v = vb[(p + 1) & 1];
-    if (p == 0) {
-      k_onesweep<true><<<grid, kSortThreads, 0, ctx->stream>>>(
-          in_k, nullptr, out_k, out_v, n, shift, scene_pass ? 1 : 0, b->d_tri_off, b->n_scenes,
-          off + (size_t)p * kRadix, lb, b->d_tile_ctr + p, ctx->d_err, ctx->spin_limit);
-    } else {
-      k_onesweep<false><<<grid, kSortThreads, 0, ctx->stream>>>(
-          in_k, in_v, out_k, out_v, n, shift, scene_pass ? 1 : 0, b->d_tri_off, b->n_scenes,
-          off + (size_t)p * kRadix, lb, b->d_tile_ctr + p, ctx->d_err, ctx->spin_limit);
-    }
+    launch_pass(ctx->stream, grid, p == 0, scene_pass, in_k, in_v, out_k, out_v, n, shift, b->d_tri_off, b->n_scenes,
+                off + (size_t)p * kRadix, lb, b->d_tile_ctr + p, ctx->d_err, ctx->spin_limit);
     FLG_LAUNCH_CHECK(ctx, "k_onesweep");
   }
   return FLG_OK;
@@ -220,14 +275,8 @@ int sort_pairs_enqueue(flg_ctx ctx, cudaStream_t st, int64_t n, int passes, uint
   FLG_LAUNCH_CHECK(ctx, "k_scan_hist");
   for (int p = 0; p < passes; ++p) {
     uint32_t *lb = lookback + (size_t)p * tiles * kRadix;
-    if (p == 0)
-      k_onesweep<true><<<(unsigned)tiles, kSortThreads, 0, st>>>(keys[0], nullptr, keys[1], vals[1], n, 0, 0, nullptr,
-                                                                  1, off, lb, tile_ctr, ctx->d_err, ctx->spin_limit);
-    else
-      k_onesweep<false><<<(unsigned)tiles, kSortThreads, 0, st>>>(keys[p & 1], vals[p & 1], keys[(p + 1) & 1],
-                                                                   vals[(p + 1) & 1], n, 8 * p, 0, nullptr, 1,
-                                                                   off + (size_t)p * kRadix, lb, tile_ctr + p,
-                                                                   ctx->d_err, ctx->spin_limit);
+    launch_pass(st, (unsigned)tiles, p == 0, false, keys[p & 1], vals[p & 1], keys[(p + 1) & 1], vals[(p + 1) & 1], n,
+                8 * p, nullptr, 1, off + (size_t)p * kRadix, lb, tile_ctr + p, ctx->d_err, ctx->spin_limit);
     FLG_LAUNCH_CHECK(ctx, "k_onesweep");
   }
   return FLG_OK;
