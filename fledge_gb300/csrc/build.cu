@@ -8,14 +8,14 @@
 //   2. k_morton_hist   30-bit Morton code per triangle (radix_bvh.cpp:63-73)
 //                      plus the digit histograms of every sort pass
 //   3. sort            onesweep radix sort (sort.cu)
-//   4. k_karras        one thread per internal node: direction, range, split
-//                      (radix_bvh.cpp:118-161) and child/parent links
-//   5. k_refit         lanes over sorted leaves: gather the triangle into the
-//                      sorted triangle array, then climb with per-node
-//                      arrival counters (radix_bvh.cpp:163-199); each child
-//                      box is written once, into its parent's record, and
-//                      the second arrival polls for its sibling's box (no
-//                      fence per level)
+//   4. k_climb         the Karras tree (radix_bvh.cpp:118-161) and its refit
+//                      (radix_bvh.cpp:163-199) in one bottom-up pass: lanes
+//                      over sorted leaves gather the triangle into the sorted
+//                      triangle array, then climb with per-node arrival
+//                      counters, choosing each node's parent from the two
+//                      neighbouring code deltas; the second arrival at a split
+//                      polls for its sibling's hand-over record (no fence per
+//                      level) and writes the finished node
 //   6. (optional) collapse to 4- or 8-wide nodes (collapse.cu)
 #include <cuda/atomic>
 
@@ -137,143 +137,112 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// delta(i, j) of radix_bvh.hpp:68-74 on a scene's sorted codes.
-struct Delta {
-  const uint32_t *code;
-  int n;
-  __device__ __forceinline__ int operator()(int i, int j) const {
-    if (j < 0 || j >= n) return -1;
-    uint32_t a = code[i], b = code[j];
-    if (a == b) return __clz((uint32_t)(i ^ j)) + 32;
-    return __clz(a ^ b);
-  }
-};
-
-__device__ __forceinline__ int next2pow(int l) {
-  return l <= 1 ? 1 : (int)(1u << (32 - __clz((uint32_t)(l - 1))));
+// delta of radix_bvh.hpp:68-74 between neighbouring sorted positions i and
+// i + 1 of a scene (codes a, b): the common prefix length of the codes, or
+// 32 + that of the positions when the codes are equal.  These are the common
+// prefixes of the distinct strings (code, position), so the Karras tree is
+// the binary radix tree over them.
+__device__ __forceinline__ int delta_next(uint32_t a, uint32_t b, int i) {
+  return a == b ? __clz((uint32_t)(i ^ (i + 1))) + 32 : __clz(a ^ b);
 }
 
-__global__ void __launch_bounds__(256)
-    k_karras(const uint32_t *__restrict__ keys, const int64_t *__restrict__ tri_off,
-             const int64_t *__restrict__ node_off, int n_scenes, int64_t n_nodes,
-             int32_t *__restrict__ split_o, uint8_t *__restrict__ leaf_o, int32_t *__restrict__ range_o,
-             int32_t *__restrict__ parent_o, int32_t *__restrict__ leaf_parent_o, Node2 *__restrict__ nodes,
-             uint32_t *__restrict__ flags_o) {
-  for (int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gi < n_nodes;
-       gi += (int64_t)gridDim.x * blockDim.x) {
-    const int s = find_segment(node_off, n_scenes, gi);
-    const int64_t toff = tri_off[s], noff = node_off[s];
-    const int n = (int)(tri_off[s + 1] - toff);
-    const int i = (int)(gi - noff);
-    Delta delta{keys + toff, n};
-    // radix_bvh.cpp:119-150
-    int dd = delta(i, i + 1) - delta(i, i - 1);
-    int d = dd == 0 ? 0 : (dd > 0 ? 1 : -1);
-    int delta_min = delta(i, i - d);
-    int l_max = 2;
-    while (delta(i, i + l_max * d) > delta_min) l_max <<= 1;
-    int l = 0;
-    for (int t = l_max >> 1; t >= 1; t >>= 1)
-      if (delta(i, i + (l + t) * d) > delta_min) l += t;
-    int j = i + l * d;
-    int delta_node = delta(i, j);
-    int sp = 0;
-    for (int t = next2pow(l); t >= 1; t >>= 1)
-      if (delta(i, i + (sp + t) * d) > delta_node) sp += t;
-    int split = i + sp * d + min(d, 0);
-    uint8_t lf = 0;
-    if (min(i, j) == split) lf |= 1;
-    if (max(i, j) == split + 1) lf |= 2;
-    split_o[gi] = split;
-    leaf_o[gi] = lf;
-    range_o[gi] = j;
-    // Parent links carry the child's side in bit 0 (0: the child at split,
-    // 1: the child at split + 1), so the refit climb needs one load a level.
-    int c0, c1;
-    if (lf & 1) {
-      c0 = ~(int)(toff + split);
-      leaf_parent_o[toff + split] = i << 1;
-    } else {
-      c0 = (int)(noff + split);
-      parent_o[noff + split] = i << 1;
-      nodes[noff + split].d.z = (int)gi;
-    }
-    if (lf & 2) {
-      c1 = ~(int)(toff + split + 1);
-      leaf_parent_o[toff + split + 1] = (i << 1) | 1;
-    } else {
-      c1 = (int)(noff + split + 1);
-      parent_o[noff + split + 1] = (i << 1) | 1;
-      nodes[noff + split + 1].d.z = (int)gi;
-    }
-    // Child boxes start as the "not yet written" pattern the refit polls on.
-    const float u = __int_as_float(kBoxUnset);
-    float4 *f4 = (float4 *)(nodes + gi);
-    f4[0] = f4[1] = f4[2] = make_float4(u, u, u, u);
-    nodes[gi].d.x = c0;
-    nodes[gi].d.y = c1;
-    nodes[gi].d.w = s;
-    flags_o[gi] = 0u;
-    if (i == 0) {
-      nodes[gi].d.z = -1;
-      parent_o[gi] = 0;
-    }
-  }
+// Side of node [l, r] of a scene of n sorted codes under its parent: 0 when
+// the parent splits at r (the node is a left child), 1 when it splits at l - 1.
+__device__ __forceinline__ int parent_side(const uint32_t *__restrict__ code, uint32_t key_l, uint32_t key_r, int l,
+                                           int r, int n) {
+  const int dr = r < n - 1 ? delta_next(key_r, code[r + 1], r) : -1;
+  const int dl = l > 0 ? delta_next(code[l - 1], key_l, l - 1) : -1;
+  return dr > dl ? 0 : 1;
 }
 
-// Child box of side s lives in float4 s (x/y lo-hi) and float2 s of the third
-// float4 (z lo-hi).  Stores and polls are relaxed device-scope accesses: the
-// climb orders nothing else through them, so no fence is needed.
-__device__ __forceinline__ void store_child_box(Node2 *nd, int side, const float *lo, const float *hi) {
-  float4 *f4 = (float4 *)nd;
-  float2 *f2 = (float2 *)(f4 + 2);
-  asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(f4 + side), "f"(lo[0]), "f"(hi[0]),
-               "f"(lo[1]), "f"(hi[1])
+// The climb's hand-over record of an internal node slot: the first child to
+// arrive leaves its box, the far end of its range and the code there; the
+// second reads it and writes the unset pattern back, so every slot is unset
+// again when a build ends (no clearing pass).  Words: lo.xyz, end | hi.xyz,
+// code; kBoxUnset is never a box word (min/max of coordinates), a range end
+// (0 .. 2^28) or a 30-bit code.
+__device__ __forceinline__ void slot_store(float4 *slot, const float *lo, const float *hi, int end,
+                                           uint32_t code) {
+  asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(slot), "f"(lo[0]), "f"(lo[1]),
+               "f"(lo[2]), "f"(__int_as_float(end))
                : "memory");
-  asm volatile("st.relaxed.gpu.global.v2.f32 [%0], {%1, %2};" ::"l"(f2 + side), "f"(lo[2]), "f"(hi[2]) : "memory");
-}
-
-// One relaxed read of a child box; true when none of its six words holds
-// kBoxUnset any more.  Each word is written once, so per-word coherence is
-// all the polling relies on (no fence orders the sibling's stores).
-__device__ __forceinline__ bool read_child_box(const Node2 *nd, int side, float *lo, float *hi) {
-  const float4 *f4 = (const float4 *)nd;
-  const float2 *f2 = (const float2 *)(f4 + 2);
-  float a0, a1, a2, a3, z0, z1;
-  asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
-               : "=f"(a0), "=f"(a1), "=f"(a2), "=f"(a3)
-               : "l"(f4 + side)
+  asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(slot + 1), "f"(hi[0]), "f"(hi[1]),
+               "f"(hi[2]), "f"(__uint_as_float(code))
                : "memory");
-  asm volatile("ld.relaxed.gpu.global.v2.f32 {%0, %1}, [%2];" : "=f"(z0), "=f"(z1) : "l"(f2 + side) : "memory");
-  lo[0] = a0; hi[0] = a1; lo[1] = a2; hi[1] = a3; lo[2] = z0; hi[2] = z1;
-  return __float_as_int(a0) != kBoxUnset && __float_as_int(a1) != kBoxUnset && __float_as_int(a2) != kBoxUnset &&
-         __float_as_int(a3) != kBoxUnset && __float_as_int(z0) != kBoxUnset && __float_as_int(z1) != kBoxUnset;
 }
 
-// Polls until read_child_box succeeds; false after `limit` polls.
-__device__ __forceinline__ bool wait_child_box(const Node2 *nd, int side, float *lo, float *hi, uint32_t limit) {
+// Polls the slot until none of its eight words is unset (per-word coherence
+// of relaxed accesses is all this relies on: each word is written once per
+// build), then resets it.  False after `limit` polls.
+__device__ __forceinline__ bool slot_take(float4 *slot, float *lo, float *hi, int &end, uint32_t &code,
+                                          uint32_t limit) {
   for (uint32_t spins = 0;; ++spins) {
-    if (read_child_box(nd, side, lo, hi)) return true;
+    float a0, a1, a2, a3, b0, b1, b2, b3;
+    asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(a0), "=f"(a1), "=f"(a2), "=f"(a3)
+                 : "l"(slot)
+                 : "memory");
+    asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(b0), "=f"(b1), "=f"(b2), "=f"(b3)
+                 : "l"(slot + 1)
+                 : "memory");
+    const bool ready = __float_as_int(a0) != kBoxUnset && __float_as_int(a1) != kBoxUnset &&
+                       __float_as_int(a2) != kBoxUnset && __float_as_int(a3) != kBoxUnset &&
+                       __float_as_int(b0) != kBoxUnset && __float_as_int(b1) != kBoxUnset &&
+                       __float_as_int(b2) != kBoxUnset && __float_as_int(b3) != kBoxUnset;
+    if (ready) {
+      lo[0] = a0; lo[1] = a1; lo[2] = a2; end = __float_as_int(a3);
+      hi[0] = b0; hi[1] = b1; hi[2] = b2; code = __float_as_uint(b3);
+      const float u = __int_as_float(kBoxUnset);
+      asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %1, %1, %1};" ::"l"(slot), "f"(u) : "memory");
+      asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %1, %1, %1};" ::"l"(slot + 1), "f"(u) : "memory");
+      return true;
+    }
     if (spins >= limit) return false;
     if (spins > 16) __nanosleep(32);
   }
 }
 
-// Bottom-up refit (radix_bvh.cpp:163-199).  Each warp owns a contiguous
-// chunk of sorted leaves.  A lane gathers its leaf's triangle into the sorted
-// triangle array, then climbs: at every node it writes its own box into the
-// parent's record and counts its arrival; the first arrival stops, the second
-// waits for the sibling's box, merges and goes on up.  Lanes that stopped
-// take new leaves together, once half the warp is idle, so that the gathers
-// of a refill run side by side on consecutive leaves.
+// Sets every climb slot to the unset pattern and every arrival counter to 0
+// (at allocation, and before a build that follows one whose climb gave up).
+__global__ void k_climb_reset(float4 *slots, uint32_t *flags, int64_t n, const uint32_t *dirty) {
+  if (dirty && *dirty == 0u) return;
+  const float u = __int_as_float(kBoxUnset);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    slots[2 * i] = slots[2 * i + 1] = make_float4(u, u, u, u);
+    flags[i] = 0u;
+  }
+}
+
+__global__ void k_climb_clean(uint32_t *dirty) { *dirty = 0u; }
+
+// Karras tree construction fused with the bottom-up refit (radix_bvh.cpp:
+// 118-199), built from the leaves up (Apetrei 2014): a node covering sorted
+// positions [l, r] of its scene is the left child of the node that splits at
+// r when delta(r, r+1) > delta(l-1, l), else the right child of the node that
+// splits at l - 1 (one of the two is the parent's split; the other lies
+// outside the parent's range and belongs to an ancestor, whose common prefix
+// is strictly shorter).  Karras numbering follows: a left child's index is its
+// right end, a right child's its left end, the root's 0 — so the second child
+// to arrive at a split knows the finished node's index as soon as it has
+// chosen that node's parent, and writes the whole Node2 there: both child
+// boxes, the child refs (split and split + 1) and the node's range.  Internal
+// node slots are numbered by sorted triangle position (node_off == tri_off),
+// so a child ref names its range boundary directly.
+//
+// Each warp owns a contiguous chunk of sorted leaves.  A lane gathers its
+// leaf's triangle into the sorted triangle array, then climbs; the first
+// child to arrive at a split (arrival counter) leaves its box in the split's
+// hand-over slot and stops, the second takes it.  Lanes that stopped take new
+// leaves together once half the warp is idle, so that the gathers of a
+// refill run side by side on consecutive leaves.
 constexpr int kRefitRefill = 16;
 
 __global__ void __launch_bounds__(256)
-    k_refit(const float *__restrict__ pos, const int32_t *__restrict__ idx, int64_t n_tri,
-            const int64_t *__restrict__ tri_off, const int64_t *__restrict__ node_off, int n_scenes,
-            const uint32_t *__restrict__ perm, const int32_t *__restrict__ parent,
-            const int32_t *__restrict__ leaf_parent, Node2 *nodes, uint32_t *flags, TriRec *__restrict__ tris,
-            uint32_t spin_limit, uint32_t *err) {
+    k_climb(const float *__restrict__ pos, const int32_t *__restrict__ idx, int64_t n_tri,
+            const int64_t *__restrict__ tri_off, int n_scenes, const uint32_t *__restrict__ keys,
+            const uint32_t *__restrict__ perm, Node2 *__restrict__ nodes, uint32_t *flags, float4 *slots,
+            TriRec *__restrict__ tris, uint32_t spin_limit, uint32_t *err, uint32_t *dirty) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt = (1u << lane) - 1u;
   const int64_t n_warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -282,8 +251,10 @@ __global__ void __launch_bounds__(256)
   int64_t next = warp * chunk;
   const int64_t end = min(next + chunk, n_tri);
   bool climbing = false;
-  int cur = 0, side = 0, n = 0, depth = 0;
-  int64_t noff = 0;
+  int n = 0, l = 0, r = 0, depth = 0;
+  int up = -1;  // side of the current node under its parent: 0 left, 1 right, -1 not chosen yet
+  int64_t toff = 0;
+  uint32_t key_l = 0, key_r = 0;
   float lo[3], hi[3];
   for (;;) {
     const unsigned idle = __ballot_sync(0xFFFFFFFFu, !climbing);
@@ -293,27 +264,27 @@ __global__ void __launch_bounds__(256)
       next += nidle;
       if (!climbing && leaf < end) {
         const int s = find_segment(tri_off, n_scenes, leaf);
-        const int64_t toff = tri_off[s];
-        noff = node_off[s];
+        toff = tri_off[s];
         n = (int)(tri_off[s + 1] - toff);
         const int64_t orig = perm[leaf];
         // A sort that timed out leaves unspecified slots: never follow them.
         if (orig < toff || orig >= toff + n) {
           atomicOr(err, kErrTimeout);
+          *dirty = 1u;
         } else {
           float3 p0, p1, p2;
           tri_verts(pos, idx, orig, p0, p1, p2);
-          TriRec r;
-          r.p0 = make_float4(p0.x, p0.y, p0.z, __int_as_float((int)(orig - toff)));
-          r.p1 = make_float4(p1.x, p1.y, p1.z, 0.0f);
-          r.p2 = make_float4(p2.x, p2.y, p2.z, 0.0f);
-          tris[leaf] = r;
+          TriRec rec;
+          rec.p0 = make_float4(p0.x, p0.y, p0.z, __int_as_float((int)(orig - toff)));
+          rec.p1 = make_float4(p1.x, p1.y, p1.z, 0.0f);
+          rec.p2 = make_float4(p2.x, p2.y, p2.z, 0.0f);
+          tris[leaf] = rec;
           if (n >= 2) {
             tri_box(p0, p1, p2, lo, hi);
-            const int ps = leaf_parent[leaf];
-            cur = ps >> 1;
-            side = ps & 1;
+            l = r = (int)(leaf - toff);
+            key_l = key_r = keys[leaf];
             depth = 0;
+            up = -1;
             climbing = true;
           }
         }
@@ -321,37 +292,69 @@ __global__ void __launch_bounds__(256)
     } else if (nidle == 32) {
       break;  // every leaf of the chunk taken and every climb finished
     }
-    if (!climbing) continue;
-    // A valid Karras tree is at most 30 + 32 levels deep; the bound only
-    // matters if the inputs were corrupted by an earlier timed-out wait.
-    if (depth > 96 || cur < 0 || cur >= n - 1) {
-      atomicOr(err, kErrTimeout);
-      climbing = false;
-      continue;
+    // Arrive: node [l, r] (a leaf or a finished internal node) at its
+    // parent's split.  Every lane passes the __syncwarp below, so a sibling
+    // in the same warp finds the first arrival's record already stored.
+    bool take = false, left = false;
+    int split = 0;
+    if (climbing) {
+      if (up < 0) up = parent_side(keys + toff, key_l, key_r, l, r, n);
+      left = up == 0;  // the parent splits at r
+      split = left ? r : l - 1;
+      // A valid tree is at most 62 levels deep; the bound only matters if the
+      // inputs were corrupted by an earlier timed-out wait.
+      if (depth > 96 || split < 0 || split >= n - 1) {
+        atomicOr(err, kErrTimeout);
+        *dirty = 1u;
+        climbing = false;
+      } else if (atomicAdd(flags + toff + split, 1u) == 0u) {
+        slot_store(slots + 2 * (toff + split), lo, hi, left ? l : r, left ? key_l : key_r);
+        climbing = false;
+      } else {
+        flags[toff + split] = 0u;  // both arrivals seen: ready for the next build
+        take = true;
+      }
     }
-    Node2 *nd = nodes + noff + cur;
-    store_child_box(nd, side, lo, hi);
-    const int ps = parent[noff + cur];  // in flight with the arrival count
-    if (atomicAdd(flags + noff + cur, 1u) == 0u) {
-      climbing = false;
-      continue;
-    }
+    __syncwarp();
+    if (!take) continue;
     float olo[3], ohi[3];
-    if (!wait_child_box(nd, side ^ 1, olo, ohi, spin_limit)) {
+    int oend = 0;
+    uint32_t okey = 0;
+    const bool got = slot_take(slots + 2 * (toff + split), olo, ohi, oend, okey, spin_limit);
+    // The new node [nl, nr] with children [nl, split] and [split + 1, nr].
+    const int nl = left ? l : oend, nr = left ? oend : r;
+    if (!got || nl < 0 || nl > split || nr <= split || nr >= n) {
       atomicOr(err, kErrTimeout);
+      *dirty = 1u;
       climbing = false;
       continue;
     }
+    if (left) key_r = okey;
+    else key_l = okey;
+    Node2 nd;
+    const float *c0lo = left ? lo : olo, *c0hi = left ? hi : ohi;
+    const float *c1lo = left ? olo : lo, *c1hi = left ? ohi : hi;
+    nd.a = make_float4(c0lo[0], c0hi[0], c0lo[1], c0hi[1]);
+    nd.b = make_float4(c1lo[0], c1hi[0], c1lo[1], c1hi[1]);
+    nd.c = make_float4(c0lo[2], c0hi[2], c1lo[2], c1hi[2]);
+    const int c0 = nl == split ? ~(int)(toff + split) : (int)(toff + split);
+    const int c1 = nr == split + 1 ? ~(int)(toff + split + 1) : (int)(toff + split + 1);
+    nd.d = make_int4(c0, c1, (int)(toff + nl), (int)(toff + nr));
+    l = nl;
+    r = nr;
     for (int k = 0; k < 3; ++k) {
       lo[k] = fminf(lo[k], olo[k]);
       hi[k] = fmaxf(hi[k], ohi[k]);
     }
-    if (cur == 0) {
-      climbing = false;
-      continue;
+    // Its Karras index: 0 for the root, else the end facing its parent.
+    int at = 0;
+    if (l == 0 && r == n - 1) {
+      climbing = false;  // the root: done
+    } else {
+      up = parent_side(keys + toff, key_l, key_r, l, r, n);
+      at = up == 0 ? r : l;
     }
-    cur = ps >> 1;
-    side = ps & 1;
+    nodes[toff + at] = nd;
     ++depth;
   }
 }
@@ -393,23 +396,22 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
     if (b->width > 2) return collapse_enqueue(ctx, b, b->width, b->leaf_size);
     return FLG_OK;
   }
-  if (b->n_nodes > 0) {
-    k_karras<<<grid_for(b->n_nodes, 256, (int64_t)ctx->num_sms * 16), 256, 0, st>>>(
-        b->d_keys, b->d_tri_off, b->d_node_off, b->n_scenes, b->n_nodes, b->d_split, b->d_leaf,
-        b->d_range_j, b->d_parent, b->d_leaf_parent, b->d_nodes2, b->d_flags);
-    FLG_LAUNCH_CHECK(ctx, "k_karras");
-  }
   // Lanes take their next leaf as soon as they stop climbing, so one wave
   // of resident CTAs balances better than more CTAs than fit.
-  static const int refit_per_sm = [] {
+  static const int climb_per_sm = [] {
     int v = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_refit, 256, 0) != cudaSuccess || v < 1) v = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_climb, 256, 0) != cudaSuccess || v < 1) v = 1;
     return v;
   }();
-  k_refit<<<grid_for(n, 256, (int64_t)ctx->num_sms * refit_per_sm), 256, 0, st>>>(
-      b->pos, b->idx, n, b->d_tri_off, b->d_node_off, b->n_scenes, b->d_perm, b->d_parent, b->d_leaf_parent,
-      b->d_nodes2, b->d_flags, b->d_tris, ctx->spin_limit, ctx->d_err);
-  FLG_LAUNCH_CHECK(ctx, "k_refit");
+  const unsigned g_nodes = grid_for(b->n_nodes, 256, (int64_t)ctx->num_sms * 8);
+  k_climb_reset<<<g_nodes, 256, 0, st>>>(b->d_slots, b->d_flags, b->n_nodes, b->d_dirty);
+  FLG_LAUNCH_CHECK(ctx, "k_climb_reset");
+  k_climb_clean<<<1, 1, 0, st>>>(b->d_dirty);
+  FLG_LAUNCH_CHECK(ctx, "k_climb_clean");
+  k_climb<<<grid_for(n, 256, (int64_t)ctx->num_sms * climb_per_sm), 256, 0, st>>>(
+      b->pos, b->idx, n, b->d_tri_off, b->n_scenes, b->d_keys, b->d_perm, b->d_nodes2, b->d_flags, b->d_slots,
+      b->d_tris, ctx->spin_limit, ctx->d_err, b->d_dirty);
+  FLG_LAUNCH_CHECK(ctx, "k_climb");
   if (b->width > 2) return collapse_enqueue(ctx, b, b->width, b->leaf_size);
   return FLG_OK;
 }
@@ -456,7 +458,7 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   std::vector<int32_t> root(n_scenes);
   for (int s = 0; s < n_scenes; ++s) {
     int64_t c = tri_off_host[s + 1] - tri_off_host[s];
-    b->node_off_h[s + 1] = b->node_off_h[s] + (c >= 2 ? c - 1 : 0);
+    b->node_off_h[s + 1] = tri_off_host[s + 1];  // node slots numbered by sorted position
     root[s] = c >= 2 ? (int32_t)b->node_off_h[s] : c == 1 ? ~(int32_t)tri_off_host[s] : INT32_MIN;
   }
   b->n_nodes = b->node_off_h[n_scenes];
@@ -479,12 +481,9 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   A(&b->d_perm, n);
   A(&b->d_keys_alt, n);
   A(&b->d_vals_alt, n);
-  A(&b->d_split, b->n_nodes);
-  A(&b->d_leaf, b->n_nodes);
-  A(&b->d_range_j, b->n_nodes);
-  A(&b->d_parent, b->n_nodes);
-  A(&b->d_leaf_parent, n);
   A(&b->d_flags, b->n_nodes);
+  A(&b->d_slots, 2 * (size_t)b->n_nodes);
+  A(&b->d_dirty, 1);
   A(&b->d_nodes2, b->n_nodes);
   A(&b->d_tris, n);
   // hist: [passes][256] counts, [passes][256] offsets, [passes][256] static scene counts
@@ -516,6 +515,14 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(b->d_hist + 512 * (size_t)b->n_passes, sh.data() + 256 * b->n_morton_passes,
                         sizeof(uint32_t) * 256 * (b->n_passes - b->n_morton_passes), cudaMemcpyHostToDevice, st);
+  // Node records zeroed (unused slots hold refs 0), climb scratch unset.
+  if (e == cudaSuccess && b->n_nodes > 0) e = cudaMemsetAsync(b->d_nodes2, 0, sizeof(Node2) * (size_t)b->n_nodes, st);
+  if (e == cudaSuccess) {
+    k_climb_reset<<<grid_for(b->n_nodes, 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(b->d_slots, b->d_flags,
+                                                                                      b->n_nodes, nullptr);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_dirty, 0, sizeof(uint32_t), st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors go out of scope
   if (e != cudaSuccess) {
     rc = cuda_fail(ctx, e, "bvh upload");
@@ -600,26 +607,46 @@ FLG_API int flg_bvh_download(flg_bvh bvh, int32_t scene, flg_bvh_topology *t) {
     return set_error(ctx, FLG_ERR_UNSUPPORTED, "only LBVH handles keep the Karras arrays");
   if (scene < 0 || scene >= bvh->n_scenes) return set_error(ctx, FLG_ERR_ARG, "scene out of range");
   cudaStream_t st = ctx->stream;
-  const int64_t toff = bvh->tri_off_h[scene], noff = bvh->node_off_h[scene];
+  const int64_t toff = bvh->tri_off_h[scene];
   const int64_t n = bvh->tri_off_h[scene + 1] - toff;
-  const int64_t m = bvh->node_off_h[scene + 1] - noff;
+  const int64_t m = n >= 2 ? n - 1 : 0;  // internal nodes, at slots toff .. toff + m - 1
   cudaError_t e = cudaStreamSynchronize(st);
   auto D = [&](void *dst, const void *src, size_t bytes) {
     if (e == cudaSuccess && dst && bytes) e = cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
   };
   D(t->morton, bvh->d_keys + toff, sizeof(uint32_t) * n);
   D(t->perm, bvh->d_perm + toff, sizeof(int32_t) * n);
-  D(t->split, bvh->d_split + noff, sizeof(int32_t) * m);
-  D(t->leaf_flags, bvh->d_leaf + noff, sizeof(uint8_t) * m);
-  D(t->range_j, bvh->d_range_j + noff, sizeof(int32_t) * m);
-  D(t->parent, bvh->d_parent + noff, sizeof(int32_t) * m);
-  D(t->leaf_parent, bvh->d_leaf_parent + toff, sizeof(int32_t) * n);
   D(t->scene_bound, bvh->d_scene_box + 6 * scene, sizeof(float) * 6);
-  if (t->bounds && m > 0) {
-    std::vector<Node2> nodes(m);
-    D(nodes.data(), bvh->d_nodes2 + noff, sizeof(Node2) * m);
-    for (int64_t i = 0; i < m && e == cudaSuccess; ++i) {
-      const Node2 &q = nodes[i];
+  std::vector<Node2> nodes(m);
+  if (m > 0) D(nodes.data(), bvh->d_nodes2 + toff, sizeof(Node2) * m);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "download");
+  if (t->perm)
+    for (int64_t i = 0; i < n; ++i) t->perm[i] -= (int32_t)toff;
+  // The Karras arrays follow from the node records: child refs name the
+  // split (left child at split, right at split + 1), d.z / d.w the range.
+  if (t->leaf_parent && n == 1) t->leaf_parent[0] = -1;  // a lone leaf is the root
+  if (t->parent && m > 0) t->parent[0] = 0;
+  for (int64_t i = 0; i < m; ++i) {
+    const Node2 &q = nodes[i];
+    const int c0 = q.d.x, c1 = q.d.y;
+    const int64_t lo = q.d.z - toff, hi = q.d.w - toff;
+    const int64_t split = (c0 >= 0 ? c0 : ~c0) - toff;
+    if (lo < 0 || hi >= n || split < lo || split >= hi || (lo != i && hi != i))
+      return set_error(ctx, FLG_ERR_STATE, "node %lld of scene %d is inconsistent", (long long)i, scene);
+    if (t->split) t->split[i] = (int32_t)split;
+    if (t->leaf_flags) t->leaf_flags[i] = (uint8_t)((c0 < 0 ? 1 : 0) | (c1 < 0 ? 2 : 0));
+    if (t->range_j) t->range_j[i] = (int32_t)(lo == i ? hi : lo);
+    const int cr[2] = {c0, c1};
+    for (int k = 0; k < 2; ++k) {
+      const int64_t c = (cr[k] >= 0 ? cr[k] : ~cr[k]) - toff;
+      if (c < 0 || c >= n) return set_error(ctx, FLG_ERR_STATE, "child ref out of scene %d", scene);
+      if (cr[k] < 0) {
+        if (t->leaf_parent) t->leaf_parent[c] = (int32_t)i;
+      } else if (t->parent && c < m) {
+        t->parent[c] = (int32_t)i;
+      }
+    }
+    if (t->bounds) {
       float *o = t->bounds + 6 * i;
       o[0] = std::min(q.a.x, q.b.x);
       o[3] = std::max(q.a.y, q.b.y);
@@ -629,14 +656,5 @@ FLG_API int flg_bvh_download(flg_bvh bvh, int32_t scene, flg_bvh_topology *t) {
       o[5] = std::max(q.c.y, q.c.w);
     }
   }
-  if (e != cudaSuccess) return cuda_fail(ctx, e, "download");
-  if (t->perm)
-    for (int64_t i = 0; i < n; ++i) t->perm[i] -= (int32_t)toff;
-  // Device parent links carry the child's side in bit 0.
-  if (t->parent)
-    for (int64_t i = 0; i < m; ++i) t->parent[i] >>= 1;
-  if (t->leaf_parent)
-    for (int64_t i = 0; i < n; ++i) t->leaf_parent[i] >>= 1;
-  if (t->leaf_parent && n == 1) t->leaf_parent[0] = -1;  // a lone leaf is the root
   return FLG_OK;
 }

@@ -27,21 +27,23 @@ __device__ __forceinline__ float half_area(const Cand &c) {
   return dx * dy + dy * dz + dz * dx;
 }
 
-// Leaf ranges of internal nodes: from the Karras range ends (range_j) or,
-// for PLOC trees, from the explicit depth-first ranges (rfirst / rcount).
+// Leaf ranges of internal nodes.  LBVH records carry their own range
+// (d.z, d.w: first and last sorted triangle) and split (the left child ref
+// names it, node slots being numbered by sorted position), so both children's
+// ranges come from the parent's record; PLOC trees keep explicit depth-first
+// ranges (rfirst / rcount) per node.
 struct Ranges {
-  const int32_t *range_j, *rfirst, *rcount;
+  const int32_t *rfirst, *rcount;
 };
 
-__device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, const Ranges &R,
-                                            const int64_t *__restrict__ tri_off,
-                                            const int64_t *__restrict__ node_off, int32_t ref, Cand &c0,
+__device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, const Ranges &R, int32_t ref, Cand &c0,
                                             Cand &c1) {
   const Node2 nd = nodes2[ref];
   int32_t r[2] = {nd.d.x, nd.d.y};
   Cand *o[2] = {&c0, &c1};
   const float lo[2][3] = {{nd.a.x, nd.a.z, nd.c.x}, {nd.b.x, nd.b.z, nd.c.z}};
   const float hi[2][3] = {{nd.a.y, nd.a.w, nd.c.y}, {nd.b.y, nd.b.w, nd.c.w}};
+  const int32_t split = r[0] >= 0 ? r[0] : ~r[0];
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
     Cand &c = *o[k];
@@ -50,19 +52,15 @@ __device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, co
       c.lo[a] = lo[k][a];
       c.hi[a] = hi[k][a];
     }
-    if (r[k] < 0) {
+    if (!R.rfirst) {
+      c.first = k == 0 ? nd.d.z : split + 1;
+      c.count = k == 0 ? split - nd.d.z + 1 : nd.d.w - split;
+    } else if (r[k] < 0) {
       c.first = ~r[k];
       c.count = 1;
-    } else if (R.rfirst) {
+    } else {
       c.first = R.rfirst[r[k]];
       c.count = R.rcount[r[k]];
-    } else {
-      const Node2 &cn = nodes2[r[k]];
-      int s = cn.d.w;
-      int li = (int)(r[k] - node_off[s]);
-      int j = R.range_j[r[k]];
-      c.first = (int32_t)tri_off[s] + min(li, j);
-      c.count = abs(li - j) + 1;
     }
   }
 }
@@ -73,8 +71,7 @@ __device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, co
 // serialised in L2.
 template <int W>
 __global__ void __launch_bounds__(128)
-    k_collapse_level(const Node2 *__restrict__ nodes2, Ranges R,
-                     const int64_t *__restrict__ tri_off, const int64_t *__restrict__ node_off, int leaf_size,
+    k_collapse_level(const Node2 *__restrict__ nodes2, Ranges R, int leaf_size,
                      const int2 *__restrict__ q_in, const int32_t *__restrict__ q_in_count, int2 *__restrict__ q_out,
                      int32_t *q_out_count, int32_t *node_ctr, int64_t cap, NodeW<W> *__restrict__ wide,
                      uint32_t *err) {
@@ -95,7 +92,7 @@ __global__ void __launch_bounds__(128)
         atomicOr(err, kErrQueue);  // a hole left by an overflowing level
       } else {
         nc = 2;
-        child_cands(nodes2, R, tri_off, node_off, item.x, c[0], c[1]);
+        child_cands(nodes2, R, item.x, c[0], c[1]);
       }
     }
     while (nc >= 2 && nc < W) {
@@ -117,7 +114,7 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
       for (int k = 0; k < W; ++k)
         if (k == best) r = c[k].ref;
-      child_cands(nodes2, R, tri_off, node_off, r, a, b);
+      child_cands(nodes2, R, r, a, b);
 #pragma unroll
       for (int k = 0; k < W; ++k) {
         if (k == best) c[k] = a;
@@ -249,9 +246,8 @@ static int collapse_levels(flg_ctx ctx, flg_bvh b) {
   // levels (millions of items in large batches), early exit on small ones.
   const unsigned grid = (unsigned)ctx->num_sms * 32;
   for (int L = 0; L < kMaxLevels; ++L) {
-    k_collapse_level<W><<<grid, 128, 0, st>>>(b->d_nodes2, Ranges{b->d_range_j, b->d_rfirst, b->d_rcount},
-                                              b->d_tri_off, b->d_node_off,
-                                              b->leaf_size, b->d_queue[L & 1], b->d_wide_ctr + 1 + L,
+    k_collapse_level<W><<<grid, 128, 0, st>>>(b->d_nodes2, Ranges{b->d_rfirst, b->d_rcount}, b->leaf_size,
+                                              b->d_queue[L & 1], b->d_wide_ctr + 1 + L,
                                               b->d_queue[(L + 1) & 1], b->d_wide_ctr + 2 + L, b->d_wide_ctr,
                                               b->wide_cap, wide, ctx->d_err);
     FLG_LAUNCH_CHECK(ctx, "k_collapse_level");

@@ -92,16 +92,14 @@ struct flg_bvh_t {
   int64_t *d_tri_off = nullptr, *d_node_off = nullptr;
   int32_t *d_root = nullptr;     // per scene: root ref (node index, ~leaf, or INT32_MIN)
   float *d_scene_box = nullptr;  // per scene: 6 floats (union of triangle boxes)
-  // Karras arrays.
+  // Sorted codes and order; internal node slots are numbered by sorted
+  // triangle position (node_off == tri_off, the last slot of a scene unused).
   uint32_t *d_keys = nullptr;    // sorted Morton codes (after build)
   uint32_t *d_perm = nullptr;    // sorted position -> original global triangle
   uint32_t *d_keys_alt = nullptr, *d_vals_alt = nullptr;
-  int32_t *d_split = nullptr;
-  uint8_t *d_leaf = nullptr;
-  int32_t *d_range_j = nullptr;
-  int32_t *d_parent = nullptr;
-  int32_t *d_leaf_parent = nullptr;
-  uint32_t *d_flags = nullptr;
+  uint32_t *d_flags = nullptr;   // climb arrival counters (0 between builds)
+  float4 *d_slots = nullptr;     // climb hand-over records, 2 per slot (unset between builds)
+  uint32_t *d_dirty = nullptr;   // a climb gave up: reset flags and slots before the next
   flg::Node2 *d_nodes2 = nullptr;
   flg::TriRec *d_tris = nullptr;
   // Sort scratch.

@@ -74,7 +74,7 @@ typedef struct flg_hits {
 typedef struct flg_build_opts {
   int32_t node_width;     /* traversal layout: 2, 4 or 8 (0 = 4) */
   int32_t leaf_size;      /* wide layouts: max triangles per leaf range (0 = 1) */
-  int32_t keep_topology;  /* keep the Karras arrays for flg_bvh_download */
+  int32_t keep_topology;  /* unused: flg_bvh_download derives the Karras arrays from the nodes */
   int32_t builder;        /* FLG_BUILDER_LBVH (0, the Karras radix tree) or FLG_BUILDER_PLOC */
 } flg_build_opts;
 
