@@ -36,9 +36,7 @@ struct Ranges {
   const int32_t *rfirst, *rcount;
 };
 
-__device__ __forceinline__ void child_cands(const Node2 *__restrict__ nodes2, const Ranges &R, int32_t ref, Cand &c0,
-                                            Cand &c1) {
-  const Node2 nd = nodes2[ref];
+__device__ __forceinline__ void child_cands(const Node2 &nd, const Ranges &R, Cand &c0, Cand &c1) {
   int32_t r[2] = {nd.d.x, nd.d.y};
   Cand *o[2] = {&c0, &c1};
   const float lo[2][3] = {{nd.a.x, nd.a.z, nd.c.x}, {nd.b.x, nd.b.z, nd.c.z}};
@@ -92,9 +90,17 @@ __global__ void __launch_bounds__(128)
         atomicOr(err, kErrQueue);  // a hole left by an overflowing level
       } else {
         nc = 2;
-        child_cands(nodes2, R, item.x, c[0], c[1]);
+        child_cands(nodes2[item.x], R, c[0], c[1]);
       }
     }
+    // The records of both children that may be opened are fetched together:
+    // the first opening takes one of them and the second usually the other,
+    // so most wide nodes wait on two dependent loads instead of three.
+    Node2 pf0, pf1;
+    const int32_t pf0_ref = nc == 2 && c[0].ref >= 0 && c[0].count > leaf_size ? c[0].ref : -1;
+    const int32_t pf1_ref = nc == 2 && c[1].ref >= 0 && c[1].count > leaf_size ? c[1].ref : -1;
+    if (pf0_ref >= 0) pf0 = nodes2[pf0_ref];
+    if (pf1_ref >= 0) pf1 = nodes2[pf1_ref];
     while (nc >= 2 && nc < W) {
       int best = -1;
       float ba = -1.0f;
@@ -114,7 +120,9 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
       for (int k = 0; k < W; ++k)
         if (k == best) r = c[k].ref;
-      child_cands(nodes2, R, r, a, b);
+      if (r == pf0_ref) child_cands(pf0, R, a, b);
+      else if (r == pf1_ref) child_cands(pf1, R, a, b);
+      else child_cands(nodes2[r], R, a, b);
 #pragma unroll
       for (int k = 0; k < W; ++k) {
         if (k == best) c[k] = a;
