@@ -250,9 +250,16 @@ template <int W>
 static int collapse_levels(flg_ctx ctx, flg_bvh b) {
   cudaStream_t st = ctx->stream;
   NodeW<W> *wide = (NodeW<W> *)b->d_wide;
-  // Level sizes are only known on the device; enough threads for the widest
-  // levels (millions of items in large batches), early exit on small ones.
-  const unsigned grid = (unsigned)ctx->num_sms * 32;
+  // Level sizes are only known on the device: one wave of resident CTAs
+  // strides over each level (no tail wave on the wide levels, a cheap
+  // launch for the empty ones after the deepest).
+  static const int per_sm = [] {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_collapse_level<W>, 128, 0) != cudaSuccess || v < 1)
+      v = 1;
+    return v;
+  }();
+  const unsigned grid = (unsigned)ctx->num_sms * (unsigned)per_sm;
   for (int L = 0; L < kMaxLevels; ++L) {
     k_collapse_level<W><<<grid, 128, 0, st>>>(b->d_nodes2, Ranges{b->d_rfirst, b->d_rcount}, b->leaf_size,
                                               b->d_queue[L & 1], b->d_wide_ctr + 1 + L,

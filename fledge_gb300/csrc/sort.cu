@@ -23,6 +23,7 @@ constexpr int kSortMinBlocks = 4;  // CTAs per SM the register budget allows
 constexpr int kSortTile = kSortThreads * kSortItems;
 constexpr int kRadix = 256;
 constexpr int kLookback = 4;  // predecessor tiles read per look-back step
+constexpr int kSceneStage = 2048;  // scene passes stage up to this many offsets in shared memory
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagPrefix = 2u << 30;
 constexpr uint32_t kFlagMask = 3u << 30;
@@ -65,10 +66,14 @@ __global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
   __shared__ int32_t s_glob[kRadix];
   __shared__ uint32_t s_wsum[kSortWarps];
   __shared__ uint32_t s_tile;
+  __shared__ int32_t s_off[kScene ? kSceneStage : 1];  // scene passes: the scene offsets
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
   for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) (&s_whist[0][0])[i] = 0u;
+  const bool staged = kScene && n_scenes <= kSceneStage;
+  if (staged)
+    for (int i = tid; i < n_scenes; i += kSortThreads) s_off[kScene ? i : 0] = (int32_t)tri_off[i];
   __syncthreads();
   const int64_t tile = s_tile;
   const int64_t base = tile * kSortTile;
@@ -88,12 +93,33 @@ __global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
     k[j] = valid ? kin[j * 32] : 0xFFFFFFFFu;
     v[j] = valid ? (kFirst ? (uint32_t)wbase + (uint32_t)(j * 32) : vin[j * 32]) : 0u;
   }
+  if (kScene) {
+    // Scene of every pair: with the offsets in shared memory, a binary search
+    // of fixed depth whose steps are interleaved over the thread's pairs
+    // (largest s with off[s] <= value, as find_segment).
+    if (staged) {
+      int sc[kScene ? kSortItems : 1];
+#pragma unroll
+      for (int j = 0; j < kSortItems; ++j) sc[kScene ? j : 0] = 0;
+      for (int step = n_scenes > 1 ? 1 << (31 - __clz(n_scenes - 1)) : 0; step >= 1; step >>= 1) {
+#pragma unroll
+        for (int j = 0; j < kSortItems; ++j) {
+          const int c = sc[kScene ? j : 0] + step;
+          if (c < n_scenes && s_off[kScene ? c : 0] <= (int32_t)v[j]) sc[kScene ? j : 0] = c;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kSortItems; ++j) dg[kScene ? j : 0] = ((uint32_t)sc[kScene ? j : 0] >> shift) & 0xFFu;
+    } else {
+#pragma unroll
+      for (int j = 0; j < kSortItems; ++j) dg[kScene ? j : 0] = sort_digit<true>(k[j], v[j], shift, tri_off, n_scenes);
+    }
+  }
   const uint32_t lt = (1u << lane) - 1u;
 #pragma unroll
   for (int j = 0; j < kSortItems; ++j) {
     const bool valid = full || j * 32 < wrem;
-    const uint32_t d = valid ? sort_digit<kScene>(k[j], v[j], shift, tri_off, n_scenes) : 256u;
-    if (kScene) dg[kScene ? j : 0] = d;
+    const uint32_t d = !valid ? 256u : kScene ? dg[kScene ? j : 0] : ((k[j] >> shift) & 0xFFu);
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
     const int leader = __ffs(peers) - 1;
     uint32_t gbase = 0u;
