@@ -30,6 +30,14 @@ namespace flg {
 
 int64_t sort_tiles(int64_t n);
 
+// Scene of triangle t given the scene `prev` of an earlier triangle of the
+// same thread (-1: none yet): one binary search, then a forward walk.
+__device__ __forceinline__ int scene_of(const int64_t *__restrict__ tri_off, int n_scenes, int64_t t, int prev) {
+  if (prev < 0) return find_segment(tri_off, n_scenes, t);
+  while (prev < n_scenes - 1 && tri_off[prev + 1] <= t) ++prev;
+  return prev;
+}
+
 // Ordered float atomics (IEEE order on the sign/magnitude encoding).
 __device__ __forceinline__ void atomic_min_f(float *a, float v) {
   if (v >= 0.0f) atomicMin((int *)a, __float_as_int(v));
@@ -110,9 +118,10 @@ __global__ void __launch_bounds__(256)
   __shared__ uint32_t s_hist[4][256];
   for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0u;
   __syncthreads();
+  int s = -1;  // scene of t: t only grows, so it is searched once and then advanced
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_tri;
        t += (int64_t)gridDim.x * blockDim.x) {
-    const int s = find_segment(tri_off, n_scenes, t);
+    s = scene_of(tri_off, n_scenes, t, s);
     float3 p0, p1, p2;
     tri_verts(pos, idx, t, p0, p1, p2);
     float lo[3], hi[3];
@@ -122,7 +131,7 @@ __global__ void __launch_bounds__(256)
     for (int k = 0; k < 3; ++k) {
       float slo = scene_box[6 * s + k], shi = scene_box[6 * s + 3 + k];
       float e = shi - slo;
-      float c = __fdiv_rn(lo[k] + hi[k], 2.0f);
+      float c = (lo[k] + hi[k]) * 0.5f;  // = the correctly rounded (lo + hi) / 2: 0.5 is exact
       float nrm = e == 0.0f ? 0.0f : __fdiv_rn(c - slo, e);
       q[k] = to_u32(nrm * 1024.0f);
     }
@@ -234,9 +243,9 @@ __global__ void k_climb_clean(uint32_t *dirty) { *dirty = 0u; }
 // leaf's triangle into the sorted triangle array, then climbs; the first
 // child to arrive at a split (arrival counter) leaves its box in the split's
 // hand-over slot and stops, the second takes it.  Lanes that stopped take new
-// leaves together once half the warp is idle, so that the gathers of a
+// leaves together once 24 of 32 lanes are idle, so that the gathers of a
 // refill run side by side on consecutive leaves.
-constexpr int kRefitRefill = 16;
+constexpr int kRefitRefill = 24;  // idle lanes before a refill: 24 beat 8 and 16
 
 __global__ void __launch_bounds__(256)
     k_climb(const float *__restrict__ pos, const int32_t *__restrict__ idx, int64_t n_tri,
@@ -253,6 +262,7 @@ __global__ void __launch_bounds__(256)
   bool climbing = false;
   int n = 0, l = 0, r = 0, depth = 0;
   int up = -1;  // side of the current node under its parent: 0 left, 1 right, -1 not chosen yet
+  int sc = -1;  // scene of the lane's last leaf (its leaves only grow)
   int64_t toff = 0;
   uint32_t key_l = 0, key_r = 0;
   float lo[3], hi[3];
@@ -263,7 +273,8 @@ __global__ void __launch_bounds__(256)
       const int64_t leaf = next + __popc(idle & lt);
       next += nidle;
       if (!climbing && leaf < end) {
-        const int s = find_segment(tri_off, n_scenes, leaf);
+        sc = scene_of(tri_off, n_scenes, leaf, sc);
+        const int s = sc;
         toff = tri_off[s];
         n = (int)(tri_off[s + 1] - toff);
         const int64_t orig = perm[leaf];
