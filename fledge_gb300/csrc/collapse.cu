@@ -14,6 +14,10 @@
 namespace flg {
 
 constexpr int kMaxLevels = 64;
+// Collapse counters: [0] wide nodes allocated, [1 + L] queue size of level L,
+// [kMaxLevels + 2 .. + 3] the one-launch collapse's barrier; the initial
+// values of these kCtrLive words follow as a static copy.
+constexpr int kCtrLive = kMaxLevels + 4;
 
 struct Cand {
   int32_t ref;     // BVH2 ref (>=0 internal, <0 ~leaf position)
@@ -63,18 +67,17 @@ __device__ __forceinline__ void child_cands(const Node2 &nd, const Ranges &R, Ca
   }
 }
 
-// One wide node per queued BVH2 node.  The new wide slots and queue entries
-// of a warp are claimed with one atomic per counter (warp prefix sum of the
-// lanes' internal children): per-child atomics on the two shared counters
-// serialised in L2.
+// One wide node per queued BVH2 node of a level (cnt items in q_in).  The
+// new wide slots and queue entries of a warp are claimed with one atomic per
+// counter (warp prefix sum of the lanes' internal children): per-child
+// atomics on the two shared counters serialised in L2.  Queue entries are
+// read through L2 (__ldcg): in the one-launch collapse this SM may still
+// hold lines of the same buffer from two levels before.
 template <int W>
-__global__ void __launch_bounds__(128)
-    k_collapse_level(const Node2 *__restrict__ nodes2, Ranges R, int leaf_size,
-                     const int2 *__restrict__ q_in, const int32_t *__restrict__ q_in_count, int2 *__restrict__ q_out,
-                     int32_t *q_out_count, int32_t *node_ctr, int64_t cap, NodeW<W> *__restrict__ wide,
-                     uint32_t *err) {
-  // Counts beyond the queue capacity only arise from a corrupted tree.
-  const int cnt = (int)min((int64_t)*q_in_count, cap);
+__device__ __forceinline__ void collapse_level(const Node2 *__restrict__ nodes2, const Ranges &R, int leaf_size,
+                                               const int2 *__restrict__ q_in, int cnt, int2 *__restrict__ q_out,
+                                               int32_t *q_out_count, int32_t *node_ctr, int64_t cap,
+                                               NodeW<W> *__restrict__ wide, uint32_t *err) {
   const int lane = threadIdx.x & 31;
   // Warp-uniform loop: all lanes of a warp share it0.
   for (int it0 = (int)((blockIdx.x * blockDim.x + threadIdx.x) & ~31u); it0 < cnt;
@@ -85,8 +88,9 @@ __global__ void __launch_bounds__(128)
     Cand c[W];
     int nc = 0;
     if (valid) {
-      item = q_in[it];
-      if (item.x < 0 || item.y < 0 || item.x >= cap || item.y >= cap) {
+      item = __ldcg(q_in + it);
+      // cap = BVH2 node count + 1: item.x names a BVH2 node, item.y a wide slot.
+      if (item.x < 0 || item.y < 0 || item.x >= cap - 1 || item.y >= cap) {
         atomicOr(err, kErrQueue);  // a hole left by an overflowing level
       } else {
         nc = 2;
@@ -185,6 +189,62 @@ __global__ void __launch_bounds__(128)
   }
 }
 
+template <int W>
+__global__ void __launch_bounds__(128)
+    k_collapse_level(const Node2 *__restrict__ nodes2, Ranges R, int leaf_size,
+                     const int2 *__restrict__ q_in, const int32_t *__restrict__ q_in_count, int2 *__restrict__ q_out,
+                     int32_t *q_out_count, int32_t *node_ctr, int64_t cap, NodeW<W> *__restrict__ wide,
+                     uint32_t *err) {
+  // Counts beyond the queue capacity only arise from a corrupted tree.
+  const int cnt = (int)min((int64_t)*q_in_count, cap);
+  collapse_level<W>(nodes2, R, leaf_size, q_in, cnt, q_out, q_out_count, node_ctr, cap, wide, err);
+}
+
+// Barrier over all CTAs of a cooperative launch (all resident): bar[0]
+// counts arrivals, bar[1] is the generation.  Fences make each CTA's writes
+// of the level visible before it arrives and the others' after it leaves.
+// The wait is bounded: on a timeout the error word is set and the CTA goes
+// on (the tree is then wrong, the device keeps answering).
+__device__ __forceinline__ void grid_barrier(uint32_t *bar, uint32_t limit, uint32_t *err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t gen = ld_volatile(bar + 1);
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      *(volatile uint32_t *)bar = 0u;
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      for (uint32_t spins = 0; ld_volatile(bar + 1) == gen; ++spins) {
+        if (spins >= limit) {
+          atomicOr(err, kErrTimeout);
+          break;
+        }
+        if (spins > 64) __nanosleep(128);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+// The whole collapse in one cooperative launch: level after level with a
+// grid barrier between them, until a level is empty.  Replaces up to 64
+// launches (most of them empty) by one.
+template <int W>
+__global__ void __launch_bounds__(128)
+    k_collapse_all(const Node2 *__restrict__ nodes2, Ranges R, int leaf_size, int2 *q0, int2 *q1, int32_t *ctr,
+                   uint32_t *bar, int64_t cap, NodeW<W> *__restrict__ wide, uint32_t spin_limit, uint32_t *err) {
+  for (int L = 0; L < kMaxLevels; ++L) {
+    // Counts beyond the queue capacity only arise from a corrupted tree.
+    const int cnt = (int)min((int64_t)(int32_t)ld_volatile((const uint32_t *)(ctr + 1 + L)), cap);
+    if (cnt == 0) break;  // the same value in every CTA: read after the last barrier
+    collapse_level<W>(nodes2, R, leaf_size, (L & 1) ? q1 : q0, cnt, (L & 1) ? q0 : q1, ctr + 2 + L, ctr, cap, wide,
+                      err);
+    grid_barrier(bar, spin_limit, err);
+  }
+}
+
 __global__ void k_collapse_check(const int32_t *last_count, uint32_t *err) {
   if (*last_count > 0) atomicOr(err, kErrQueue);
 }
@@ -208,7 +268,7 @@ int collapse_reserve(flg_ctx ctx, flg_bvh b) {
   b->wide_rec = (int64_t)rec;
   if (!b->d_wide_root) {
     if ((rc = halloc(b, &b->d_wide_root, b->n_scenes))) return rc;
-    if ((rc = halloc(b, &b->d_wide_ctr, 2 * (kMaxLevels + 2)))) return rc;
+    if ((rc = halloc(b, &b->d_wide_ctr, 2 * kCtrLive))) return rc;
     if ((rc = halloc(b, &b->d_queue[0], cap))) return rc;
     if ((rc = halloc(b, &b->d_queue[1], cap))) return rc;
     if ((rc = halloc(b, &b->d_queue_init, b->n_scenes))) return rc;
@@ -226,13 +286,11 @@ int collapse_reserve(flg_ctx ctx, flg_bvh b) {
       }
     }
     b->n_wide_roots = (int32_t)q.size();
-    // counters: [0] nodes, [1 + L] queue size of level L; a static copy of
-    // the initial values follows at [kMaxLevels + 2].
-    std::vector<int32_t> ctr(2 * (kMaxLevels + 2), 0);
+    std::vector<int32_t> ctr(2 * kCtrLive, 0);
     ctr[0] = b->n_wide_roots;
     ctr[1] = b->n_wide_roots;
-    ctr[kMaxLevels + 2] = b->n_wide_roots;
-    ctr[kMaxLevels + 3] = b->n_wide_roots;
+    ctr[kCtrLive] = b->n_wide_roots;
+    ctr[kCtrLive + 1] = b->n_wide_roots;
     cudaStream_t st = ctx->stream;
     cudaError_t e = cudaMemcpyAsync(b->d_wide_root, roots.data(), sizeof(int32_t) * b->n_scenes,
                                     cudaMemcpyHostToDevice, st);
@@ -250,24 +308,51 @@ template <int W>
 static int collapse_levels(flg_ctx ctx, flg_bvh b) {
   cudaStream_t st = ctx->stream;
   NodeW<W> *wide = (NodeW<W> *)b->d_wide;
-  // Level sizes are only known on the device: one wave of resident CTAs
-  // strides over each level (no tail wave on the wide levels, a cheap
-  // launch for the empty ones after the deepest).
-  static const int per_sm = [] {
+  const Ranges R{b->d_rfirst, b->d_rcount};
+  // Level sizes are only known on the device.  Default: one cooperative
+  // launch of one resident wave that walks the levels with a grid barrier in
+  // between and stops at the first empty one.  Under stream capture: one
+  // launch of one resident wave per level (the empty ones after the deepest
+  // exit at once).
+  static const int all_per_sm = [] {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_collapse_all<W>, 128, 0) != cudaSuccess || v < 1)
+      v = 1;
+    return v;
+  }();
+  static const int level_per_sm = [] {
     int v = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_collapse_level<W>, 128, 0) != cudaSuccess || v < 1)
       v = 1;
     return v;
   }();
-  const unsigned grid = (unsigned)ctx->num_sms * (unsigned)per_sm;
-  for (int L = 0; L < kMaxLevels; ++L) {
-    k_collapse_level<W><<<grid, 128, 0, st>>>(b->d_nodes2, Ranges{b->d_rfirst, b->d_rcount}, b->leaf_size,
-                                              b->d_queue[L & 1], b->d_wide_ctr + 1 + L,
-                                              b->d_queue[(L + 1) & 1], b->d_wide_ctr + 2 + L, b->d_wide_ctr,
-                                              b->wide_cap, wide, ctx->d_err);
-    FLG_LAUNCH_CHECK(ctx, "k_collapse_level");
+  int32_t *ctr = b->d_wide_ctr;
+  if (!ctx->capturing) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)ctx->num_sms * (unsigned)all_per_sm);
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    uint32_t *bar = (uint32_t *)(ctr + kMaxLevels + 2);
+    FLG_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_collapse_all<W>, (const Node2 *)b->d_nodes2, R, (int)b->leaf_size,
+                                     b->d_queue[0], b->d_queue[1], ctr, bar, (int64_t)b->wide_cap, wide,
+                                     ctx->spin_limit, ctx->d_err));
+    FLG_LAUNCH_CHECK(ctx, "k_collapse_all");
+  } else {
+    const unsigned grid = (unsigned)ctx->num_sms * (unsigned)level_per_sm;
+    for (int L = 0; L < kMaxLevels; ++L) {
+      k_collapse_level<W><<<grid, 128, 0, st>>>(b->d_nodes2, R, b->leaf_size, b->d_queue[L & 1], ctr + 1 + L,
+                                                b->d_queue[(L + 1) & 1], ctr + 2 + L, ctr, b->wide_cap, wide,
+                                                ctx->d_err);
+      FLG_LAUNCH_CHECK(ctx, "k_collapse_level");
+    }
   }
-  k_collapse_check<<<1, 1, 0, st>>>(b->d_wide_ctr + 1 + kMaxLevels, ctx->d_err);
+  k_collapse_check<<<1, 1, 0, st>>>(ctr + 1 + kMaxLevels, ctx->d_err);
   FLG_LAUNCH_CHECK(ctx, "k_collapse_check");
   return FLG_OK;
 }
@@ -276,8 +361,8 @@ int collapse_enqueue(flg_ctx ctx, flg_bvh b, int width, int leaf_size) {
   (void)leaf_size;
   if (b->n_wide_roots == 0) return FLG_OK;
   cudaStream_t st = ctx->stream;
-  FLG_CUDA(ctx, cudaMemcpyAsync(b->d_wide_ctr, b->d_wide_ctr + kMaxLevels + 2,
-                                sizeof(int32_t) * (kMaxLevels + 2), cudaMemcpyDeviceToDevice, st));
+  FLG_CUDA(ctx, cudaMemcpyAsync(b->d_wide_ctr, b->d_wide_ctr + kCtrLive, sizeof(int32_t) * kCtrLive,
+                                cudaMemcpyDeviceToDevice, st));
   FLG_CUDA(ctx, cudaMemcpyAsync(b->d_queue[0], b->d_queue_init, sizeof(int2) * b->n_wide_roots,
                                 cudaMemcpyDeviceToDevice, st));
   return width == 4 ? collapse_levels<4>(ctx, b) : collapse_levels<8>(ctx, b);
