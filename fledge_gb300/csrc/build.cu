@@ -109,8 +109,27 @@ __global__ void __launch_bounds__(kBoundsThreads)
   }
 }
 
-// Morton code of every triangle against its scene box (radix_bvh.cpp:63-73,
-// experimental_utils.hpp:33-45) and the per-pass digit histograms.
+// Morton code of triangle t against its scene box sb (radix_bvh.cpp:63-73,
+// experimental_utils.hpp:33-45).
+__device__ __forceinline__ uint32_t morton_of(const float *__restrict__ pos, const int32_t *__restrict__ idx,
+                                              int64_t t, const float *__restrict__ sb) {
+  float3 p0, p1, p2;
+  tri_verts(pos, idx, t, p0, p1, p2);
+  float lo[3], hi[3];
+  tri_box(p0, p1, p2, lo, hi);
+  uint32_t q[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float slo = sb[k], shi = sb[3 + k];
+    float e = shi - slo;
+    float c = (lo[k] + hi[k]) * 0.5f;  // = the correctly rounded (lo + hi) / 2: 0.5 is exact
+    float nrm = e == 0.0f ? 0.0f : __fdiv_rn(c - slo, e);
+    q[k] = to_u32(nrm * 1024.0f);
+  }
+  return (left_shift3(q[2]) << 2) | (left_shift3(q[1]) << 1) | left_shift3(q[0]);
+}
+
+// Morton code of every triangle and the per-pass digit histograms.
 __global__ void __launch_bounds__(256)
     k_morton_hist(const float *__restrict__ pos, const int32_t *__restrict__ idx, int64_t n_tri,
                   const int64_t *__restrict__ tri_off, int n_scenes, const float *__restrict__ scene_box,
@@ -122,20 +141,7 @@ __global__ void __launch_bounds__(256)
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n_tri;
        t += (int64_t)gridDim.x * blockDim.x) {
     s = scene_of(tri_off, n_scenes, t, s);
-    float3 p0, p1, p2;
-    tri_verts(pos, idx, t, p0, p1, p2);
-    float lo[3], hi[3];
-    tri_box(p0, p1, p2, lo, hi);
-    uint32_t q[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      float slo = scene_box[6 * s + k], shi = scene_box[6 * s + 3 + k];
-      float e = shi - slo;
-      float c = (lo[k] + hi[k]) * 0.5f;  // = the correctly rounded (lo + hi) / 2: 0.5 is exact
-      float nrm = e == 0.0f ? 0.0f : __fdiv_rn(c - slo, e);
-      q[k] = to_u32(nrm * 1024.0f);
-    }
-    uint32_t code = (left_shift3(q[2]) << 2) | (left_shift3(q[1]) << 1) | left_shift3(q[0]);
+    const uint32_t code = morton_of(pos, idx, t, scene_box + 6 * s);
     keys[t] = code;
     for (int p = 0; p < n_hist_passes; ++p) atomicAdd(&s_hist[p][(code >> (8 * p)) & 0xFFu], 1u);
   }
@@ -144,6 +150,58 @@ __global__ void __launch_bounds__(256)
     uint32_t c = (&s_hist[0][0])[i];
     if (c) atomicAdd(&hist[i], c);
   }
+}
+
+// Segmented sorts (batched builds whose scenes span several sort tiles): one
+// block per sort tile, tiles aligned to scenes (tile_start[s] = first tile of
+// scene s), so each block adds its codes' digit counts to its own scene's
+// histograms hist[s][pass][digit].
+__global__ void __launch_bounds__(256)
+    k_morton_seg(const float *__restrict__ pos, const int32_t *__restrict__ idx, const int64_t *__restrict__ tri_off,
+                 int n_scenes, const int32_t *__restrict__ tile_start, int tile, const float *__restrict__ scene_box,
+                 uint32_t *__restrict__ keys, uint32_t *__restrict__ hist) {
+  __shared__ uint32_t s_hist[4][256];
+  __shared__ int s_scene;
+  for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0u;
+  if (threadIdx.x == 0) s_scene = find_segment32(tile_start, n_scenes, (int32_t)blockIdx.x);
+  __syncthreads();
+  const int s = s_scene;
+  const int64_t base = tri_off[s] + (int64_t)(blockIdx.x - tile_start[s]) * tile;
+  const int64_t end = min(base + tile, tri_off[s + 1]);
+  const float *sb = scene_box + 6 * s;
+  for (int64_t t = base + threadIdx.x; t < end; t += blockDim.x) {
+    const uint32_t code = morton_of(pos, idx, t, sb);
+    keys[t] = code;
+#pragma unroll
+    for (int p = 0; p < 4; ++p) atomicAdd(&s_hist[p][(code >> (8 * p)) & 0xFFu], 1u);
+  }
+  __syncthreads();
+  uint32_t *h = hist + (size_t)s * 4 * 256;
+  for (int i = threadIdx.x; i < 4 * 256; i += blockDim.x) {
+    const uint32_t c = (&s_hist[0][0])[i];
+    if (c) atomicAdd(&h[i], c);
+  }
+}
+
+// Exclusive scan of each scene's digit counts per pass, offset by the
+// scene's first position: the global start of every (scene, pass, digit)
+// bucket.  One block of 256 threads per (scene, pass).
+__global__ void k_scan_seg(const uint32_t *__restrict__ hist, const int64_t *__restrict__ tri_off,
+                           uint32_t *__restrict__ off) {
+  __shared__ uint32_t s_w[8];
+  const int sp = blockIdx.x, d = threadIdx.x, lane = d & 31, warp = d >> 5;
+  const uint32_t c = hist[(size_t)sp * 256 + d];
+  uint32_t x = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[warp] = x;
+  __syncthreads();
+  uint32_t pre = 0;
+  for (int w = 0; w < warp; ++w) pre += s_w[w];
+  off[(size_t)sp * 256 + d] = (uint32_t)tri_off[sp / 4] + pre + x - c;
 }
 
 // delta of radix_bvh.hpp:68-74 between neighbouring sorted positions i and
@@ -381,7 +439,11 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
   const unsigned fill_grid = grid_for(b->n_scenes, 128);
   k_init_boxes<<<fill_grid, 128, 0, st>>>(b->d_scene_box, b->n_scenes);
   FLG_LAUNCH_CHECK(ctx, "k_init_boxes");
-  FLG_CUDA(ctx, cudaMemsetAsync(b->d_hist, 0, sizeof(uint32_t) * 256 * b->n_morton_passes, st));
+  if (b->d_tile_start) {
+    FLG_CUDA(ctx, cudaMemsetAsync(b->d_shist, 0, sizeof(uint32_t) * 4 * 256 * (size_t)b->n_scenes, st));
+  } else {
+    FLG_CUDA(ctx, cudaMemsetAsync(b->d_hist, 0, sizeof(uint32_t) * 256 * b->n_morton_passes, st));
+  }
   if (b->n_passes > b->n_morton_passes)
     FLG_CUDA(ctx, cudaMemcpyAsync(b->d_hist + 256 * b->n_morton_passes,
                                   b->d_hist + 512 * b->n_passes,
@@ -395,10 +457,19 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
                                                                      b->n_scenes, b->d_scene_box);
   FLG_LAUNCH_CHECK(ctx, "k_scene_bounds");
   uint32_t *morton_out = (b->n_passes % 2 == 0) ? b->d_keys : b->d_keys_alt;
-  const unsigned g_elem = grid_for(n, 256, (int64_t)ctx->num_sms * 8);
-  k_morton_hist<<<g_elem, 256, 0, st>>>(b->pos, b->idx, n, b->d_tri_off, b->n_scenes, b->d_scene_box,
-                                        morton_out, b->d_hist, b->n_morton_passes);
-  FLG_LAUNCH_CHECK(ctx, "k_morton_hist");
+  if (b->d_tile_start) {
+    k_morton_seg<<<(unsigned)b->n_tiles, 256, 0, st>>>(b->pos, b->idx, b->d_tri_off, b->n_scenes, b->d_tile_start,
+                                                      (int)sort_tile(), b->d_scene_box, morton_out, b->d_shist);
+    FLG_LAUNCH_CHECK(ctx, "k_morton_seg");
+    k_scan_seg<<<(unsigned)(4 * b->n_scenes), 256, 0, st>>>(b->d_shist, b->d_tri_off,
+                                                             b->d_shist + 4 * 256 * (size_t)b->n_scenes);
+    FLG_LAUNCH_CHECK(ctx, "k_scan_seg");
+  } else {
+    const unsigned g_elem = grid_for(n, 256, (int64_t)ctx->num_sms * 8);
+    k_morton_hist<<<g_elem, 256, 0, st>>>(b->pos, b->idx, n, b->d_tri_off, b->n_scenes, b->d_scene_box,
+                                          morton_out, b->d_hist, b->n_morton_passes);
+    FLG_LAUNCH_CHECK(ctx, "k_morton_hist");
+  }
   int rc = sort_enqueue(ctx, b);
   if (rc) return rc;
   if (b->builder == FLG_BUILDER_PLOC) {
@@ -477,8 +548,20 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   b->n_morton_passes = 4;
   int scene_passes = 0;
   if (n_scenes > 1) scene_passes = n_scenes <= 256 ? 1 : n_scenes <= 65536 ? 2 : 3;
-  b->n_passes = b->n_morton_passes + scene_passes;
   b->n_tiles = sort_tiles(n);
+  // Batched builds whose scenes average at least 4 sort tiles sort each
+  // scene in its own run of tiles (per-scene digit offsets, look-back chains
+  // restarting at each scene) instead of appending scene passes.
+  std::vector<int32_t> tile_start;
+  if (n_scenes > 1 && n >= 4 * (int64_t)sort_tile() * n_scenes) {
+    tile_start.resize(n_scenes + 1);
+    tile_start[0] = 0;
+    for (int s = 0; s < n_scenes; ++s)
+      tile_start[s + 1] = tile_start[s] + (int32_t)sort_tiles(tri_off_host[s + 1] - tri_off_host[s]);
+    b->n_tiles = tile_start[n_scenes];
+    scene_passes = 0;
+  }
+  b->n_passes = b->n_morton_passes + scene_passes;
 
   int rc = FLG_OK;
   auto A = [&](auto **p, size_t c) {
@@ -499,6 +582,10 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   A(&b->d_tris, n);
   // hist: [passes][256] counts, [passes][256] offsets, [passes][256] static scene counts
   A(&b->d_hist, 3 * 256 * (size_t)b->n_passes);
+  if (!tile_start.empty()) {
+    A(&b->d_tile_start, n_scenes + 1);
+    A(&b->d_shist, 2 * 4 * 256 * (size_t)n_scenes);  // per-scene counts, then bucket starts
+  }
   A(&b->d_lookback, 256 * (size_t)b->n_tiles * b->n_passes);
   A(&b->d_tile_ctr, b->n_passes);
   if (rc == FLG_OK && builder == FLG_BUILDER_PLOC) rc = ploc_reserve(b);
@@ -521,6 +608,9 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
                         cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(b->d_root, root.data(), sizeof(int32_t) * n_scenes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && !tile_start.empty())
+    e = cudaMemcpyAsync(b->d_tile_start, tile_start.data(), sizeof(int32_t) * (n_scenes + 1),
+                        cudaMemcpyHostToDevice, st);
   // Static scene counts live after counts and offsets; build_enqueue copies
   // the scene passes' part into place each build.
   if (e == cudaSuccess)

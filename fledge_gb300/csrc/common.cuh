@@ -367,6 +367,16 @@ __device__ __forceinline__ int find_segment(const int64_t *off, int n_seg, int64
   return lo;
 }
 
+// find_segment over 32-bit offsets.
+__device__ __forceinline__ int find_segment32(const int32_t *off, int n_seg, int32_t x) {
+  int lo = 0, hi = n_seg - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 // Vertices of triangle t of a soup (idx NULL) or an indexed mesh.
 __device__ __forceinline__ void tri_verts(const float *__restrict__ pos, const int32_t *__restrict__ idx,
                                           int64_t t, float3 &a, float3 &b, float3 &c) {

@@ -108,6 +108,10 @@ struct flg_bvh_t {
   uint32_t *d_tile_ctr = nullptr;  // [passes]
   int32_t n_passes = 0, n_morton_passes = 0;
   int64_t n_tiles = 0;
+  // Segmented sorts: first sort tile of every scene (n_scenes + 1), per-scene
+  // digit counts [scene][pass][256] followed by the buckets' global starts.
+  int32_t *d_tile_start = nullptr;
+  uint32_t *d_shist = nullptr;
   std::vector<uint32_t> scene_hist_h;  // scene-digit histograms (host)
   // Wide layout.
   int32_t width = 2, leaf_size = 1;
@@ -203,6 +207,7 @@ int collapse_reserve(flg_ctx ctx, flg_bvh b);
 int collapse_enqueue(flg_ctx ctx, flg_bvh b, int width, int leaf_size);
 int sort_enqueue(flg_ctx ctx, flg_bvh b);
 int64_t sort_tiles(int64_t n);
+int64_t sort_tile();  // pairs per sort tile
 int sort_pairs_enqueue(flg_ctx ctx, cudaStream_t st, int64_t n, int passes, uint32_t *const keys[2],
                        uint32_t *const vals[2], uint32_t *hist, uint32_t *lookback, uint32_t *tile_ctr);
 int ploc_reserve(flg_bvh b);

@@ -9,8 +9,11 @@
 // shared-memory atomics, publishes its per-digit counts,
 // resolves its global offsets by looking back over earlier tiles, reorders
 // the tile in shared memory and writes runs of equal digits contiguously.
-// Batched builds append passes whose digit is the scene of the pair (from
-// the triangle offsets), which regroups the scenes after the Morton passes.
+// Batched builds either sort every scene in its own run of tiles (per-scene
+// digit offsets, look-back chains restarting at each scene's first tile: when
+// scenes average at least 4 tiles) or append passes whose digit is the scene
+// of the pair (from the triangle offsets), which regroup the scenes after the
+// Morton passes.
 #include "common.cuh"
 #include "internal.h"
 
@@ -59,7 +62,8 @@ __global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
     k_onesweep(const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int64_t n, int shift,
                const int64_t *__restrict__ tri_off, int n_scenes, const uint32_t *__restrict__ pass_off,
-               uint32_t *lookback, uint32_t *tile_ctr, uint32_t *err, uint32_t spin_limit) {
+               const int32_t *__restrict__ tile_start, int64_t scene_stride, uint32_t *lookback, uint32_t *tile_ctr,
+               uint32_t *err, uint32_t spin_limit) {
   __shared__ uint2 s_kv[kSortTile];
   __shared__ uint8_t s_dig[kScene ? kSortTile : 1];
   __shared__ uint32_t s_whist[kSortWarps][kRadix];
@@ -67,20 +71,34 @@ __global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
   __shared__ uint32_t s_wsum[kSortWarps];
   __shared__ uint32_t s_tile;
   __shared__ int32_t s_off[kScene ? kSceneStage : 1];  // scene passes: the scene offsets
+  __shared__ int32_t s_seg;                             // segmented sorts: the tile's scene
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
+  if (tid == 0) {
+    s_tile = atomicAdd(tile_ctr, 1u);
+    if (tile_start) s_seg = find_segment32(tile_start, n_scenes, (int32_t)s_tile);
+  }
   for (int i = tid; i < kSortWarps * kRadix; i += kSortThreads) (&s_whist[0][0])[i] = 0u;
   const bool staged = kScene && n_scenes <= kSceneStage;
   if (staged)
     for (int i = tid; i < n_scenes; i += kSortThreads) s_off[kScene ? i : 0] = (int32_t)tri_off[i];
   __syncthreads();
   const int64_t tile = s_tile;
-  const int64_t base = tile * kSortTile;
-  const bool full = base + kSortTile <= n;
+  // A segmented sort keeps every scene in its own run of tiles: the tile
+  // covers part of [tri_off[s], tri_off[s+1]), the look-back stops at the
+  // scene's first tile and the digit offsets are the scene's.
+  int64_t first_tile = 0, base = tile * kSortTile, seg_end = n;
+  if (tile_start) {
+    const int sc = s_seg;
+    first_tile = tile_start[sc];
+    base = tri_off[sc] + (tile - first_tile) * kSortTile;
+    seg_end = tri_off[sc + 1];
+    pass_off += (size_t)sc * scene_stride;
+  }
+  const bool full = base + kSortTile <= seg_end;
   const int64_t wbase = base + (int64_t)warp * (kSortItems * 32) + lane;
   // Pairs of this lane left in the input, as a 32-bit bound for the checks.
-  const int64_t wrem64 = n - wbase;
+  const int64_t wrem64 = seg_end - wbase;
   const int wrem = wrem64 > kSortTile ? kSortTile : (wrem64 < 0 ? 0 : (int)wrem64);
   const uint32_t *kin = keys_in + wbase;
   const uint32_t *vin = kFirst ? nullptr : vals_in + wbase;
@@ -139,7 +157,7 @@ __global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
     tile_count += c;
   }
   uint32_t *lb = lookback + (size_t)tile * kRadix;
-  st_volatile(lb + d, tile_count | (tile == 0 ? kFlagPrefix : kFlagAgg));
+  st_volatile(lb + d, tile_count | (tile == first_tile ? kFlagPrefix : kFlagAgg));
 
   // Exclusive scan of the tile counts over digits: the digit's start in the
   // tile's shared-memory reorder, added to every warp's offset.
@@ -164,22 +182,23 @@ __global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
   // have only published aggregates costs m / kLookback L2 round trips instead
   // of m.  A word read early stays usable (an aggregate never changes; only
   // its flag may since have become a prefix); an unpublished one is waited
-  // on.  Tile 0 always holds a prefix, so the walk ends there at the latest.
+  // on.  The first tile (of the scene) always holds a prefix, so the walk
+  // ends there at the latest.
   // Each wait is bounded: on a timeout the error word is set and a (wrong)
   // prefix is still published so later tiles do not wait on this one;
   // writes stay bounds-checked.
   uint32_t excl = 0;
-  if (tile > 0) {
+  if (tile > first_tile) {
     int64_t p = tile - 1;
     bool done = false;
     while (!done) {
       uint32_t s[kLookback];
 #pragma unroll
       for (int i = 0; i < kLookback; ++i)
-        s[i] = p - i >= 0 ? ld_volatile(lookback + (size_t)(p - i) * kRadix + d) : 0u;
+        s[i] = p - i >= first_tile ? ld_volatile(lookback + (size_t)(p - i) * kRadix + d) : 0u;
 #pragma unroll
       for (int i = 0; i < kLookback; ++i) {
-        if (!done && p - i >= 0) {
+        if (!done && p - i >= first_tile) {
           uint32_t w = s[i];
           if (!(w & kFlagMask)) w = wait_flag(lookback + (size_t)(p - i) * kRadix + d, kFlagMask, spin_limit, err);
           excl += w & kValMask;
@@ -187,7 +206,7 @@ __global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
         }
       }
       p -= kLookback;
-      if (p < 0) done = true;
+      if (p < first_tile) done = true;
     }
     st_volatile(lb + d, ((excl + tile_count) & kValMask) | kFlagPrefix);
   }
@@ -204,7 +223,7 @@ __global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
     }
   }
   __syncthreads();
-  const int64_t rem = n - base;
+  const int64_t rem = seg_end - base;
   const int tile_valid = rem < kSortTile ? (int)rem : kSortTile;
   for (int i = tid; i < tile_valid; i += kSortThreads) {
     const uint2 kv = s_kv[i];
@@ -220,20 +239,24 @@ __global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
 // Launches one pass (the template pair for first / scene passes).
 static void launch_pass(cudaStream_t st, unsigned grid, bool first, bool scene, const uint32_t *in_k,
                         const uint32_t *in_v, uint32_t *out_k, uint32_t *out_v, int64_t n, int shift,
-                        const int64_t *tri_off, int n_scenes, const uint32_t *pass_off, uint32_t *lb,
-                        uint32_t *tile_ctr, uint32_t *err, uint32_t spin_limit) {
+                        const int64_t *tri_off, int n_scenes, const uint32_t *pass_off, const int32_t *tile_start,
+                        int64_t scene_stride, uint32_t *lb, uint32_t *tile_ctr, uint32_t *err, uint32_t spin_limit) {
   if (first && scene)
     k_onesweep<true, true><<<grid, kSortThreads, 0, st>>>(in_k, in_v, out_k, out_v, n, shift, tri_off, n_scenes,
-                                                          pass_off, lb, tile_ctr, err, spin_limit);
+                                                          pass_off, tile_start, scene_stride, lb, tile_ctr, err,
+                                                          spin_limit);
   else if (first)
     k_onesweep<true, false><<<grid, kSortThreads, 0, st>>>(in_k, in_v, out_k, out_v, n, shift, tri_off, n_scenes,
-                                                           pass_off, lb, tile_ctr, err, spin_limit);
+                                                           pass_off, tile_start, scene_stride, lb, tile_ctr, err,
+                                                           spin_limit);
   else if (scene)
     k_onesweep<false, true><<<grid, kSortThreads, 0, st>>>(in_k, in_v, out_k, out_v, n, shift, tri_off, n_scenes,
-                                                           pass_off, lb, tile_ctr, err, spin_limit);
+                                                           pass_off, tile_start, scene_stride, lb, tile_ctr, err,
+                                                           spin_limit);
   else
     k_onesweep<false, false><<<grid, kSortThreads, 0, st>>>(in_k, in_v, out_k, out_v, n, shift, tri_off, n_scenes,
-                                                            pass_off, lb, tile_ctr, err, spin_limit);
+                                                            pass_off, tile_start, scene_stride, lb, tile_ctr, err,
+                                                            spin_limit);
 }
 
 // Exclusive scan of each pass's 256 digit counts (one block per pass).
@@ -255,6 +278,7 @@ __global__ void k_scan_hist(const uint32_t *__restrict__ hist, uint32_t *__restr
 }
 
 int64_t sort_tiles(int64_t n) { return ceil_div(n, kSortTile); }
+int64_t sort_tile() { return kSortTile; }
 
 // Enqueues the passes.  Expects: b->d_kbuf[0] holds the unsorted codes and
 // b->d_hist[0 .. n_morton_passes) the code histograms; the scene-pass
@@ -265,8 +289,16 @@ int sort_enqueue(flg_ctx ctx, flg_bvh b) {
   if (n <= 0) return FLG_OK;
   uint32_t *hist = b->d_hist;
   uint32_t *off = b->d_hist + (size_t)b->n_passes * kRadix;
-  k_scan_hist<<<b->n_passes, kRadix, 0, ctx->stream>>>(hist, off);
-  FLG_LAUNCH_CHECK(ctx, "k_scan_hist");
+  int64_t scene_stride = 0;
+  if (b->d_tile_start) {
+    // Segmented: the bucket starts are per scene ([scene][pass][digit], from
+    // k_scan_seg).
+    off = b->d_shist + 4 * kRadix * (size_t)b->n_scenes;
+    scene_stride = 4 * kRadix;
+  } else {
+    k_scan_hist<<<b->n_passes, kRadix, 0, ctx->stream>>>(hist, off);
+    FLG_LAUNCH_CHECK(ctx, "k_scan_hist");
+  }
   const unsigned grid = (unsigned)b->n_tiles;
   // Ping-pong: pass p reads buffer (p & 1) and writes buffer ((p + 1) & 1).
   uint32_t *kb[2] = {b->n_passes % 2 == 0 ? b->d_keys : b->d_keys_alt,
@@ -280,7 +312,8 @@ int sort_enqueue(flg_ctx ctx, flg_bvh b) {
     uint32_t *in_k = kb[p & 1], *out_k = kb[(p + 1) & 1];
     uint32_t *in_v = vb[p & 1], *out_v = vb[(p + 1) & 1];
     launch_pass(ctx->stream, grid, p == 0, scene_pass, in_k, in_v, out_k, out_v, n, shift, b->d_tri_off, b->n_scenes,
-                off + (size_t)p * kRadix, lb, b->d_tile_ctr + p, ctx->d_err, ctx->spin_limit);
+                off + (size_t)p * kRadix, b->d_tile_start, scene_stride, lb, b->d_tile_ctr + p, ctx->d_err,
+                ctx->spin_limit);
     FLG_LAUNCH_CHECK(ctx, "k_onesweep");
   }
   return FLG_OK;
@@ -302,7 +335,8 @@ int sort_pairs_enqueue(flg_ctx ctx, cudaStream_t st, int64_t n, int passes, uint
   for (int p = 0; p < passes; ++p) {
     uint32_t *lb = lookback + (size_t)p * tiles * kRadix;
     launch_pass(st, (unsigned)tiles, p == 0, false, keys[p & 1], vals[p & 1], keys[(p + 1) & 1], vals[(p + 1) & 1], n,
-                8 * p, nullptr, 1, off + (size_t)p * kRadix, lb, tile_ctr + p, ctx->d_err, ctx->spin_limit);
+                8 * p, nullptr, 1, off + (size_t)p * kRadix, nullptr, 0, lb, tile_ctr + p, ctx->d_err,
+                ctx->spin_limit);
     FLG_LAUNCH_CHECK(ctx, "k_onesweep");
   }
   return FLG_OK;

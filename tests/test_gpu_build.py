@@ -130,3 +130,24 @@ def test_batched_build_300_scenes(ctx, oracle):
     bb.build()
     for s in (0, 1, 255, 256, 299):
         U.assert_same_topology(bb.topology(s), oracle.build_bvh(pos[3 * offs[s]:3 * offs[s + 1]]))
+
+
+@pytest.mark.gpu
+def test_batched_build_segmented_sort(ctx, oracle):
+    """Scenes averaging at least 4 sort tiles (3072 pairs each) are sorted in
+    their own runs of tiles, with per-scene digit offsets and look-back
+    chains: empty scenes, a one-triangle scene, a scene of exactly one tile,
+    one just over a tile boundary and large ones between them."""
+    import fledge_gb300 as F
+    rng = np.random.default_rng(29)
+    counts = [40000, 0, 1, 3072, 3073, 0, 65536, 25000, 2]
+    assert sum(counts) >= 4 * 3072 * len(counts)
+    offs = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    pos = G.random_soup(int(offs[-1]), rng)
+    bb = F.BatchedRadixBVHBuilder(F.InternalTriangleMesh(U.dev(pos)), offs, ctx, node_width=2)
+    for _ in range(2):  # a rebuild reuses the per-scene histograms and look-back words
+        bb.build()
+        for s, c in enumerate(counts):
+            if c == 0:
+                continue
+            U.assert_same_topology(bb.topology(s), oracle.build_bvh(pos[3 * offs[s]:3 * offs[s + 1]]))
