@@ -129,22 +129,26 @@ __device__ __forceinline__ float3 camera_dir(const PtScene &S, float x, float y)
                             S.fwd[2] + xo * S.right[2] + yo * S.up[2]));
 }
 
+// A wavefront carries the paths of K consecutive samples s0 .. s0 + K - 1:
+// path p = j * n_pix + pixel is sample s0 + j of that pixel.
 struct PtQueues {
   float *rx[2][6];           // ray queues A/B: ox oy oz dx dy dz
-  int32_t *path[2];          // queue slot -> path (pixel) index
+  int32_t *path[2];          // queue slot -> path index
   float *sx[7];              // shadow queue: ox oy oz dx dy dz tmax
   float *scontrib;           // 3 per shadow slot
-  int32_t *spix;             // pixel of a shadow slot
+  int32_t *spath;            // path of a shadow slot
   float *beta;               // 3 per path
+  float *rad;                // 3 per path: the path's radiance (each path adds to its own, no atomics)
   int32_t *cnt;              // Halton dimensions consumed, per path
   int32_t *cnt_end;          // dimension count at the end of sample 0, per pixel
   int32_t *counts;           // [0] queue B size, [1] shadow size
+  int32_t n_pix;             // pixels per sample
 };
 
-__global__ void k_pt_camera(PtScene S, Halton H, int s, PtQueues Q, int qa) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int n = S.width * S.height;
-  if (i >= n) return;
+__global__ void k_pt_camera(PtScene S, Halton H, int s0, int n_path, PtQueues Q, int qa) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n_path) return;
+  const int i = p % Q.n_pix, s = s0 + p / Q.n_pix;
   const int x = i % S.width, y = i / S.width;
   const uint64_t off = halton_pixel_offset(H, x, y);
   float px, py;
@@ -163,15 +167,16 @@ __global__ void k_pt_camera(PtScene S, Halton H, int s, PtQueues Q, int qa) {
     cnt += 2;
   }
   const float3 d = camera_dir(S, px, py);
-  Q.rx[qa][0][i] = S.eye[0];
-  Q.rx[qa][1][i] = S.eye[1];
-  Q.rx[qa][2][i] = S.eye[2];
-  Q.rx[qa][3][i] = d.x;
-  Q.rx[qa][4][i] = d.y;
-  Q.rx[qa][5][i] = d.z;
-  Q.path[qa][i] = i;
-  Q.beta[3 * i] = Q.beta[3 * i + 1] = Q.beta[3 * i + 2] = 1.0f;
-  Q.cnt[i] = cnt;
+  Q.rx[qa][0][p] = S.eye[0];
+  Q.rx[qa][1][p] = S.eye[1];
+  Q.rx[qa][2][p] = S.eye[2];
+  Q.rx[qa][3][p] = d.x;
+  Q.rx[qa][4][p] = d.y;
+  Q.rx[qa][5][p] = d.z;
+  Q.path[qa][p] = p;
+  Q.beta[3 * p] = Q.beta[3 * p + 1] = Q.beta[3 * p + 2] = 1.0f;
+  Q.rad[3 * p] = Q.rad[3 * p + 1] = Q.rad[3 * p + 2] = 0.0f;
+  Q.cnt[p] = cnt;
 }
 
 // Warp-aggregated slot in a compacted queue.
@@ -194,23 +199,25 @@ __device__ __forceinline__ int queue_slot(bool want, int32_t *counter) {
 // factor; the shadow ray's transmittance is applied in k_pt_shadow); the
 // continuation ray (cosine-weighted bounce or HGSampleP).
 __global__ void __launch_bounds__(256)
-    k_pt_shade(PtScene S, Halton H, int s, int depth, int64_t n_in, PtQueues Q, int qa, const int32_t *__restrict__ prim,
-               const float *__restrict__ th, const float *__restrict__ uh, const float *__restrict__ vh, float *radiance) {
+    k_pt_shade(PtScene S, Halton H, int s0, int depth, int64_t n_in, PtQueues Q, int qa, const int32_t *__restrict__ prim,
+               const float *__restrict__ th, const float *__restrict__ uh, const float *__restrict__ vh) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = q < n_in;
   const int qb = qa ^ 1;
-  int pix = 0, cnt = 0;
+  int pid = 0, pix = 0, s = 0, cnt = 0;
   bool cont = false, shadow = false;
   float3 o = make_float3(0.f, 0.f, 0.f), d = o, beta = make_float3(1.f, 1.f, 1.f);
   float3 so = o, sd = o, contrib = o, nd = o, no = o;
   float smax = 0.0f;
   const float inv_spp = 1.0f / (float)S.spp;
   if (valid) {
-    pix = Q.path[qa][q];
+    pid = Q.path[qa][q];
+    pix = pid % Q.n_pix;
+    s = s0 + pid / Q.n_pix;
     o = make_float3(Q.rx[qa][0][q], Q.rx[qa][1][q], Q.rx[qa][2][q]);
     d = make_float3(Q.rx[qa][3][q], Q.rx[qa][4][q], Q.rx[qa][5][q]);
-    beta = make_float3(Q.beta[3 * pix], Q.beta[3 * pix + 1], Q.beta[3 * pix + 2]);
-    cnt = Q.cnt[pix];
+    beta = make_float3(Q.beta[3 * pid], Q.beta[3 * pid + 1], Q.beta[3 * pid + 2]);
+    cnt = Q.cnt[pid];
     const int32_t h = prim[q];
     const int x = pix % S.width, y = pix / S.width;
     const uint64_t off = halton_pixel_offset(H, x, y);
@@ -224,9 +231,9 @@ __global__ void __launch_bounds__(256)
       const bool is_light = h >= S.light_first && h < S.light_first + S.light_count;
       // emission seen directly (bounces == 0); AreaLight::L (light.cpp:76-79)
       if (depth == 0 && is_light && f3dot(ng, make_float3(-d.x, -d.y, -d.z)) > 0.0f) {
-        atomicAdd(radiance + 3 * pix, beta.x * S.le[0] * inv_spp);
-        atomicAdd(radiance + 3 * pix + 1, beta.y * S.le[1] * inv_spp);
-        atomicAdd(radiance + 3 * pix + 2, beta.z * S.le[2] * inv_spp);
+        Q.rad[3 * pid] += beta.x * S.le[0] * inv_spp;
+        Q.rad[3 * pid + 1] += beta.y * S.le[1] * inv_spp;
+        Q.rad[3 * pid + 2] += beta.z * S.le[2] * inv_spp;
       }
       if (depth < S.max_depth) {
         const float3 wo = make_float3(-d.x, -d.y, -d.z);
@@ -335,28 +342,28 @@ __global__ void __launch_bounds__(256)
     Q.scontrib[3 * ss] = contrib.x;
     Q.scontrib[3 * ss + 1] = contrib.y;
     Q.scontrib[3 * ss + 2] = contrib.z;
-    Q.spix[ss] = pix;
+    Q.spath[ss] = pid;
   }
   const int ns = queue_slot(valid && cont, Q.counts);
   if (ns >= 0) {
     Q.rx[qb][0][ns] = no.x; Q.rx[qb][1][ns] = no.y; Q.rx[qb][2][ns] = no.z;
     Q.rx[qb][3][ns] = nd.x; Q.rx[qb][4][ns] = nd.y; Q.rx[qb][5][ns] = nd.z;
-    Q.path[qb][ns] = pix;
-    Q.beta[3 * pix] = beta.x;
-    Q.beta[3 * pix + 1] = beta.y;
-    Q.beta[3 * pix + 2] = beta.z;
-    Q.cnt[pix] = cnt;
+    Q.path[qb][ns] = pid;
+    Q.beta[3 * pid] = beta.x;
+    Q.beta[3 * pid + 1] = beta.y;
+    Q.beta[3 * pid + 2] = beta.z;
+    Q.cnt[pid] = cnt;
   }
 }
 
 // Unoccluded shadow rays add their contribution; with a medium, times the
 // ratio-tracking transmittance of the shadow segment (VolEstimateTr,
 // integrator.cpp:40-66).
-__global__ void k_pt_shadow(PtScene S, int s, int depth, int64_t n, const uint8_t *__restrict__ occ, PtQueues Q,
-                            float *radiance) {
+__global__ void k_pt_shadow(PtScene S, int s0, int depth, int64_t n, const uint8_t *__restrict__ occ, PtQueues Q) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || occ[i]) return;
-  const int p = Q.spix[i];
+  const int pid = Q.spath[i];
+  const int p = pid % Q.n_pix, s = s0 + pid / Q.n_pix;
   float tr = 1.0f;
   if (S.medium) {
     const float3 o = make_float3(Q.sx[0][i], Q.sx[1][i], Q.sx[2][i]);
@@ -370,9 +377,20 @@ __global__ void k_pt_shadow(PtScene S, int s, int depth, int64_t n, const uint8_
                                        ct, ck, cc);
     if (tr == 0.0f) return;
   }
-  atomicAdd(radiance + 3 * p, Q.scontrib[3 * i] * tr);
-  atomicAdd(radiance + 3 * p + 1, Q.scontrib[3 * i + 1] * tr);
-  atomicAdd(radiance + 3 * p + 2, Q.scontrib[3 * i + 2] * tr);
+  // A path has at most one shadow ray per bounce: no other thread adds to it.
+  Q.rad[3 * pid] += Q.scontrib[3 * i] * tr;
+  Q.rad[3 * pid + 1] += Q.scontrib[3 * i + 1] * tr;
+  Q.rad[3 * pid + 2] += Q.scontrib[3 * i + 2] * tr;
+}
+
+// Adds the wavefront's K samples of every pixel to the image, in sample
+// order (a fixed summation order: the image does not depend on scheduling).
+__global__ void k_pt_reduce(const float *__restrict__ rad, int n_pix, int k_samples, float *radiance) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // pixel * 3 + channel
+  if (e >= 3 * (int64_t)n_pix) return;
+  float acc = radiance[e];
+  for (int j = 0; j < k_samples; ++j) acc += rad[(int64_t)j * 3 * n_pix + e];
+  radiance[e] = acc;
 }
 
 static void host_halton(int width, int height, Halton &H) {
@@ -481,11 +499,16 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
   host_halton(cam->width, cam->height, H);
 
   const int64_t n = (int64_t)cam->width * cam->height;
-  // Buffers: 2 x 6 ray arrays, 2 path maps, 7 shadow arrays + 3 contrib + pix,
-  // beta 3, cnt, cnt_end, hits 4, occluded, counters: 30 sub-buffers, each
-  // rounded up to 256 bytes.
-  const size_t fl = sizeof(float) * n;
-  const size_t need = fl * (12 + 2 + 7 + 3 + 1 + 3 + 1 + 1 + 4) + n + 64 + 32 * 256;
+  // Samples per wavefront: sample 0 alone (sample 1 continues its Halton
+  // dimensions), then up to kmax at a time, with up to 2^25 paths in flight,
+  // so every bounce's trace launches fill the GPU.
+  const int64_t kmax = std::max<int64_t>(1, std::min<int64_t>(spp, ((int64_t)1 << 25) / n));
+  const int64_t np = kmax * n;  // path slots
+  // Buffers (per path slot): 2 x 6 ray arrays, 2 path maps, 7 shadow arrays
+  // + 3 contrib + path, beta 3, radiance 3, cnt, hits 4, occluded; cnt_end per
+  // pixel; counters.  Each sub-buffer is rounded up to 256 bytes.
+  const size_t fl = sizeof(float) * np;
+  const size_t need = fl * (12 + 2 + 7 + 3 + 1 + 3 + 3 + 1 + 4) + sizeof(int32_t) * n + np + 64 + 32 * 256;
   if (ctx->pt_bytes < need) {
     cudaFree(ctx->pt_buf);
     ctx->pt_buf = nullptr;
@@ -500,41 +523,45 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
     return (void *)p;
   };
   PtQueues Q;
+  Q.n_pix = (int32_t)n;
   for (int a = 0; a < 2; ++a)
     for (int k = 0; k < 6; ++k) Q.rx[a][k] = (float *)take(fl);
   Q.path[0] = (int32_t *)take(fl);
   Q.path[1] = (int32_t *)take(fl);
   for (int k = 0; k < 7; ++k) Q.sx[k] = (float *)take(fl);
   Q.scontrib = (float *)take(3 * fl);
-  Q.spix = (int32_t *)take(fl);
+  Q.spath = (int32_t *)take(fl);
   Q.beta = (float *)take(3 * fl);
+  Q.rad = (float *)take(3 * fl);
   Q.cnt = (int32_t *)take(fl);
-  Q.cnt_end = (int32_t *)take(fl);
+  Q.cnt_end = (int32_t *)take(sizeof(int32_t) * n);
   float *hbuf = (float *)take(4 * fl);
-  uint8_t *occ = (uint8_t *)take(n);
+  uint8_t *occ = (uint8_t *)take(np);
   Q.counts = (int32_t *)take(64);
   if (bp > (char *)ctx->pt_buf + need) return set_error(ctx, FLG_ERR_STATE, "internal buffer layout");
 
   cudaStream_t st = ctx->stream;
-  FLG_CUDA(ctx, cudaMemsetAsync(radiance, 0, 3 * fl, st));
+  FLG_CUDA(ctx, cudaMemsetAsync(radiance, 0, 3 * sizeof(float) * n, st));
   int64_t n_closest = 0, n_shadow = 0;
   int32_t counts[2];
-  for (int s = 0; s < spp; ++s) {
+  for (int s0 = 0; s0 < spp;) {
+    const int k = s0 == 0 ? 1 : (int)std::min<int64_t>(kmax, spp - s0);
+    const int64_t n_path = (int64_t)k * n;
     int qa = 0;
-    k_pt_camera<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(S, H, s, Q, qa);
+    k_pt_camera<<<(unsigned)ceil_div(n_path, 256), 256, 0, st>>>(S, H, s0, (int)n_path, Q, qa);
     FLG_LAUNCH_CHECK(ctx, "k_pt_camera");
-    int64_t n_a = n;
+    int64_t n_a = n_path;
     for (int depth = 0; depth <= max_depth && n_a > 0; ++depth) {
       // t > 0 as the live renderer's Triangle::intersect (shape.cpp:100-148)
       flg_rays rr{Q.rx[qa][0], Q.rx[qa][1], Q.rx[qa][2], Q.rx[qa][3], Q.rx[qa][4], Q.rx[qa][5], nullptr, nullptr,
                   1e-30f, 3.402823466e+38f};
-      flg_hits hh{(int32_t *)hbuf, hbuf + n, hbuf + 2 * n, hbuf + 3 * n};
+      flg_hits hh{(int32_t *)hbuf, hbuf + np, hbuf + 2 * np, hbuf + 3 * np};
       int rc = trace_enqueue(ctx, st, 0, bvh, &rr, n_a, opts, nullptr, 1, &hh, nullptr);
       if (rc) return rc;
       n_closest += n_a;
       FLG_CUDA(ctx, cudaMemsetAsync(Q.counts, 0, 2 * sizeof(int32_t), st));
-      k_pt_shade<<<(unsigned)ceil_div(n_a, 256), 256, 0, st>>>(S, H, s, depth, n_a, Q, qa, hh.prim, hh.t, hh.u, hh.v,
-                                                                radiance);
+      k_pt_shade<<<(unsigned)ceil_div(n_a, 256), 256, 0, st>>>(S, H, s0, depth, n_a, Q, qa, hh.prim, hh.t, hh.u,
+                                                                hh.v);
       FLG_LAUNCH_CHECK(ctx, "k_pt_shade");
       FLG_CUDA(ctx, cudaMemcpyAsync(counts, Q.counts, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
       FLG_CUDA(ctx, cudaStreamSynchronize(st));
@@ -543,12 +570,15 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
         rc = trace_enqueue(ctx, st, 0, bvh, &sr, counts[1], opts, nullptr, 1, nullptr, occ);
         if (rc) return rc;
         n_shadow += counts[1];
-        k_pt_shadow<<<(unsigned)ceil_div(counts[1], 256), 256, 0, st>>>(S, s, depth, counts[1], occ, Q, radiance);
+        k_pt_shadow<<<(unsigned)ceil_div(counts[1], 256), 256, 0, st>>>(S, s0, depth, counts[1], occ, Q);
         FLG_LAUNCH_CHECK(ctx, "k_pt_shadow");
       }
       n_a = counts[0];
       qa ^= 1;
     }
+    k_pt_reduce<<<(unsigned)ceil_div(3 * n, 256), 256, 0, st>>>(Q.rad, (int)n, k, radiance);
+    FLG_LAUNCH_CHECK(ctx, "k_pt_reduce");
+    s0 += k;
   }
   if (stats) {
     stats->closest_rays = n_closest;
