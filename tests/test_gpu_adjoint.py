@@ -38,7 +38,7 @@ def test_hit_adjoint_matches_fp64_oracle(ctx, oracle, indexed):
     prim = h["prim"].cpu().numpy()
     n_tri = ind.shape[0] if ind is not None else pos.shape[0] // 3
     go = oracle.hit_adjoint64(pos, ind, n_tri, pos.reshape(-1, 3).shape[0], rays, prim, *g.cpu().numpy())
-    # fp32 adjoint vs FP64: the bar of the benchmark spec (1e-3 relative)
+    # fp32 adjoint vs FP64: gradients must agree to 1e-3 relative
     err = np.linalg.norm(gh - go) / np.linalg.norm(go)
     assert err < 1e-3, err
 
