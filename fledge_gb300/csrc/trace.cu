@@ -108,26 +108,47 @@ __device__ __forceinline__ uint64_t stack_key(float t, int32_t ref) {
 // vertices for the float-float refinement of t, u, v.  The traversal keeps
 // only t; the fp32 barycentrics (pluecker) are formed here, for the winner,
 // and replaced by the refined ones unless the refinement finds den == 0.
+// Result of a finished ray.  Closest hits store the sorted position of the
+// triangle and the fp32 t; k_trace_finish turns them into the original id
+// and the refined t, u, v afterwards.  Refining here cost several hundred
+// instructions per ray, run whenever a ray retired, i.e. with few lanes of
+// the warp active: about a fifth of the traversal kernel's issue slots.
 __device__ __forceinline__ void write_result(const Out &O, int64_t i, bool any, bool have, int32_t prim,
-                                             float best, float tmax, const TriRec *__restrict__ tris,
-                                             const float3 &o, const float3 &d) {
-  float u = 0.0f, v = 0.0f;
+                                             float best, float tmax) {
   if (any) {
     O.occ[i] = have ? 1 : 0;
   } else {
-    if (have) {
-      const float4 *p = (const float4 *)(tris + prim);
-      const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
-      const float3 pa = make_float3(a.x, a.y, a.z), pb = make_float3(b.x, b.y, b.z), pc = make_float3(c.x, c.y, c.z);
-      float tf;
-      pluecker(pa, pb, pc, o, d, tf, u, v);
-      refine_tuv(pa, pb, pc, o, d, best, u, v);
-      prim = __float_as_int(a.w);
-    }
     O.prim[i] = have ? prim : -1;
     O.t[i] = have ? best : tmax;
-    O.u[i] = have ? u : 0.0f;
-    O.v[i] = have ? v : 0.0f;
+    if (!have) {
+      O.u[i] = 0.0f;
+      O.v[i] = 0.0f;
+    }
+  }
+}
+
+// Hit values of every closest hit, one ray per thread after the traversal
+// (same ray floats, same triangle record, same arithmetic as in the loop):
+// barycentrics from the Pluecker quantities, then t, u, v recomputed in
+// float-float and rounded once (refine_tuv); the sorted position becomes
+// the caller's triangle id.
+__global__ void __launch_bounds__(256)
+    k_trace_finish(RaySoA R, int64_t n, Out O, const TriRec *__restrict__ tris) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t g = O.prim[i];
+    if (g < 0) continue;
+    const float3 o = make_float3(__ldg(R.ox + i), __ldg(R.oy + i), __ldg(R.oz + i));
+    const float3 d = make_float3(__ldg(R.dx + i), __ldg(R.dy + i), __ldg(R.dz + i));
+    const float4 *p = (const float4 *)(tris + g);
+    const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    const float3 pa = make_float3(a.x, a.y, a.z), pb = make_float3(b.x, b.y, b.z), pc = make_float3(c.x, c.y, c.z);
+    float best = O.t[i], u = 0.0f, v = 0.0f, tf;
+    pluecker(pa, pb, pc, o, d, tf, u, v);
+    refine_tuv(pa, pb, pc, o, d, best, u, v);
+    O.prim[i] = __float_as_int(a.w);
+    O.t[i] = best;
+    O.u[i] = u;
+    O.v[i] = v;
   }
 }
 
@@ -218,7 +239,7 @@ __global__ void __launch_bounds__(256)
     record_overflow(S, i);
     return;
   }
-  write_result(O, i, ANY, have, prim, best, tmax, tris, o, d);
+  write_result(O, i, ANY, have, prim, best, tmax);
 }
 
 // ----------------------------------------------------------------------------
@@ -400,7 +421,7 @@ __global__ void __launch_bounds__(256)
   while (!tr.step(nodes, tris)) {
   }
   if (tr.overflow) record_overflow(S, i);
-  else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tris, tr.o, tr.d);
+  else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax);
 }
 
 template <int W, bool ANY, int STACK>
@@ -437,7 +458,7 @@ __global__ void __launch_bounds__(256)
     }
     if (active && tr.step(nodes, tris)) {
       if (tr.overflow) record_overflow(S, ray);
-      else write_result(O, ray, ANY, tr.have, tr.prim, tr.best, tr.tmax, tris, tr.o, tr.d);
+      else write_result(O, ray, ANY, tr.have, tr.prim, tr.best, tr.tmax);
       active = false;
     }
   }
@@ -464,7 +485,7 @@ __global__ void __launch_bounds__(128)
         atomicOr(S.err, kErrStack);
         continue;
       }
-      write_result(O, i, ANY, have, prim, best, tmax, tris, o, d);
+      write_result(O, i, ANY, have, prim, best, tmax);
     } else {
       Tracer<(W == 2 ? 4 : W), ANY, kRetryStack> tr;
       tr.o = o; tr.d = d; tr.inv = inv; tr.tmin = tmin; tr.tmax = tmax;
@@ -472,7 +493,7 @@ __global__ void __launch_bounds__(128)
       while (!tr.step(nodes, tris)) {
       }
       if (tr.overflow) atomicOr(S.err, kErrStack);
-      else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax, tris, tr.o, tr.d);
+      else write_result(O, i, ANY, tr.have, tr.prim, tr.best, tr.tmax);
     }
   }
 }
@@ -643,7 +664,7 @@ __global__ void __launch_bounds__(256, 4)
     // Retire finished rays.
     if (active && cur == kNone && leaf == kNone && leaf2 == kNone) {
       if (overflow) record_overflow(S, ray);
-      else write_result(O, ray, ANY, have, prim, best, tmax, tris, o, d);
+      else write_result(O, ray, ANY, have, prim, best, tmax);
       active = false;
     }
     // Refill idle lanes.
@@ -793,6 +814,15 @@ static void launch_wide(flg_ctx ctx, cudaStream_t st, flg_bvh b, const RaySoA &R
 }
 
 // Enqueues one traversal of n rays on stream st with scratch set `set`.
+// Closest hits: the hit-value pass after every traversal kernel of a call.
+static int finish_enqueue(flg_ctx ctx, cudaStream_t st, const RaySoA &R, int64_t n, const Out &O, flg_bvh b,
+                          bool any) {
+  if (any || n <= 0) return FLG_OK;
+  k_trace_finish<<<grid_for(n, 256, (int64_t)ctx->num_sms * 16), 256, 0, st>>>(R, n, O, b->d_tris);
+  FLG_LAUNCH_CHECK(ctx, "k_trace_finish");
+  return FLG_OK;
+}
+
 int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_rays *rays, int64_t n,
                   const flg_trace_opts *opts, const int64_t *ray_off_dev, int n_scenes, flg_hits *hits,
                   uint8_t *occ) {
@@ -889,7 +919,7 @@ int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_ra
       k_trace_retry<2, false, true><<<rg, 128, 0, st>>>(nullptr, b->d_nodes2, b->d_tris, b->d_root, ray_off_dev,
                                                         n_scenes, R, O, S);
     FLG_LAUNCH_CHECK(ctx, "trace retry kernel");
-    return FLG_OK;
+    return finish_enqueue(ctx, st, R, n, O, b, any);
   }
   if (b->width == 2) {
     const unsigned g = (unsigned)ceil_div(n, 256);
@@ -924,7 +954,7 @@ int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_ra
   }
 #undef FLG_RETRY
   FLG_LAUNCH_CHECK(ctx, "trace retry kernel");
-  return FLG_OK;
+  return finish_enqueue(ctx, st, R, n, O, b, any);
 }
 
 }  // namespace flg
@@ -1250,5 +1280,5 @@ FLG_API int flg_trace_closest_noalloc(flg_ctx ctx, flg_bvh bvh, const flg_rays *
                                                 bvh->d_wide_root, nullptr, 1, R, O, S);
   }
   FLG_LAUNCH_CHECK(ctx, "k_trace_retry");
-  return FLG_OK;
+  return finish_enqueue(ctx, st, R, n, O, bvh, false);
 }
