@@ -63,6 +63,21 @@ __device__ __forceinline__ int32_t scene_root(const int32_t *__restrict__ roots,
   return __ldg(roots + s);
 }
 
+// The same for a lane whose rays only grow (persistent kernels take them
+// from one counter): `sc` holds the scene of the lane's previous ray (-1:
+// none yet); one search, then a forward walk.
+__device__ __forceinline__ int32_t scene_root_walk(const int32_t *__restrict__ roots,
+                                                   const int64_t *__restrict__ ray_off, int n_scenes, int64_t i,
+                                                   int &sc) {
+  if (!ray_off) return __ldg(roots);
+  if (sc < 0) {
+    sc = find_segment(ray_off, n_scenes, i);
+  } else {
+    while (sc < n_scenes - 1 && __ldg(ray_off + sc + 1) <= i) ++sc;
+  }
+  return __ldg(roots + sc);
+}
+
 // Tests sorted triangle g; updates the closest hit.  Returns true on accept.
 // MT selects the live renderer's Moller-Trumbore test and its strict
 // t < tMax rule instead of the watertight Pluecker test.
@@ -434,6 +449,7 @@ __global__ void __launch_bounds__(256)
   Tracer<W, ANY, STACK> tr;
   bool active = false, exhausted = false;
   int64_t ray = -1;
+  int scene = -1;
   while (true) {
     const unsigned idle = __ballot_sync(0xFFFFFFFFu, !active);
     const int nidle = __popc(idle);
@@ -446,7 +462,7 @@ __global__ void __launch_bounds__(256)
         if (my < n) {
           ray = my;
           load_ray(R, ray, tr.o, tr.d, tr.inv, tr.tmin, tr.tmax);
-          tr.start(scene_root(roots, ray_off, n_scenes, ray));
+          tr.start(scene_root_walk(roots, ray_off, n_scenes, ray, scene));
           active = true;
         }
       }
@@ -630,7 +646,7 @@ __global__ void __launch_bounds__(256, 4)
   float3 o = make_float3(0.f, 0.f, 0.f), d = o, inv = o;
   float tmin = 0.f, tmax = 0.f, best = 0.f;
   int32_t prim = -1, cur = kNone, leaf = kNone, leaf2 = kNone;
-  int sp = 0;
+  int sp = 0, scene = -1;
   bool have = false, active = false, overflow = false, exhausted = false;
   int64_t ray = -1;
   // Two-level stack: the top kStackTop entries of every lane live in shared
@@ -686,7 +702,7 @@ __global__ void __launch_bounds__(256, 4)
           sp = 0;
           leaf = kNone;
           leaf2 = kNone;
-          cur = scene_root(roots, ray_off, n_scenes, ray);
+          cur = scene_root_walk(roots, ray_off, n_scenes, ray, scene);
           if (cur == INT32_MIN) cur = kNone;
           active = true;
         }
