@@ -314,7 +314,10 @@ __device__ __forceinline__ uint64_t key_entry(uint32_t key, const int32_t (&ref)
 // slab1 disappears; the products are the same roundings, so tnear and the
 // hit decision equal slab_tnear's (a NaN slab, 0 * inf, constrains nothing
 // in both).  Returns the number of children hit with tnear <= lim; their
-// keys are in key[] (misses are ~0), the child refs in ref[].
+// keys are in key[] (misses are ~0), the child refs in ref[] — loaded only
+// when a child is hit (the kernel is bound by L1 throughput; skipping that
+// 16-byte load on visits without hits gave +2.5 %).  Empty slots need no
+// test of their ref: they hold +inf boxes, which no ray enters.
 template <int W>
 __device__ __forceinline__ int visit_node(const NodeW<W> *__restrict__ node, const float3 &o, const float3 &inv,
                                           float lim, uint32_t (&key)[W], int32_t (&ref)[W]) {
@@ -330,17 +333,14 @@ __device__ __forceinline__ int visit_node(const NodeW<W> *__restrict__ node, con
     const float4 a = __ldg(np + nx + h), b = __ldg(np + (nx ^ Q) + h);
     const float4 c = __ldg(np + ny + h), e = __ldg(np + (ny ^ Q) + h);
     const float4 f = __ldg(np + nz + h), g = __ldg(np + (nz ^ Q) + h);
-    const int4 r = __ldg((const int4 *)np + 6 * Q + h);
     const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
     const float cv[4] = {c.x, c.y, c.z, c.w}, ev[4] = {e.x, e.y, e.z, e.w};
     const float fv[4] = {f.x, f.y, f.z, f.w}, gv[4] = {g.x, g.y, g.z, g.w};
-    const int32_t rv[4] = {r.x, r.y, r.z, r.w};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       pn[0][4 * h + k] = av[k]; pf[0][4 * h + k] = bv[k];
       pn[1][4 * h + k] = cv[k]; pf[1][4 * h + k] = ev[k];
       pn[2][4 * h + k] = fv[k]; pf[2][4 * h + k] = gv[k];
-      ref[4 * h + k] = rv[k];
     }
   }
   const float t1c = fminf(lim, 3.402823466e+38f);
@@ -352,9 +352,16 @@ __device__ __forceinline__ int visit_node(const NodeW<W> *__restrict__ node, con
     const float tnz = (pn[2][k] - o.z) * inv.z, tfz = (pf[2][k] - o.z) * inv.z;
     const float t0 = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
     const float t1 = fminf(fminf(tfx, tfy), fminf(tfz, t1c));
-    const bool ok = ref[k] != kEmptyChild && t0 <= t1;
+    const bool ok = t0 <= t1;  // empty slots hold +inf boxes, which no ray enters
     key[k] = ok ? ((__float_as_uint(t0) & 0x7FFFFFFFu & ~(uint32_t)(W - 1)) | (uint32_t)k) : ~0u;
     nh += ok ? 1 : 0;
+  }
+  if (nh > 0) {
+#pragma unroll
+    for (int h = 0; h < Q; ++h) {
+      const int4 r = __ldg((const int4 *)np + 6 * Q + h);
+      ref[4 * h] = r.x; ref[4 * h + 1] = r.y; ref[4 * h + 2] = r.z; ref[4 * h + 3] = r.w;
+    }
   }
   return nh;
 }
