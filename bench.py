@@ -749,7 +749,8 @@ def main() -> None:
     ap.add_argument("--width", type=int, default=4)
     # defaults: the fastest setting of the sweep over node width, leaf size,
     # kernel kind and refill threshold on the first 32 scenes
-    ap.add_argument("--leaf", type=int, default=2)
+    # leaf ranges of up to 3 triangles: 1244 Mrays/s against 1166 for 2, 1017 for 1 and 1232 for 4
+    ap.add_argument("--leaf", type=int, default=3)
     ap.add_argument("--refill", type=int, default=8)
     ap.add_argument("--persistent", type=int, default=2)
     ap.add_argument("--stack", type=int, default=64)
