@@ -46,7 +46,7 @@ BYTES_PER_TRI_BATCHED = 36 + 44 + (8 + 5 * 24) + 20 + 100
 # (profiles/k_trace_ww_w4_config3_8scenes.md: dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch over the first 8 scenes, divided by its
 # 41,186,368 rays); scaled by rays to a full launch.
-TRACE_DRAM_BYTES_PER_RAY_NCU = (1.413264e9 + 0.703824e9) / 41186368
+TRACE_DRAM_BYTES_PER_RAY_NCU = (1.259081e9 + 0.378162e9) / 41186368
 
 
 _T0 = time.perf_counter()
