@@ -1115,8 +1115,8 @@ FLG_API int flg_autotune_trace(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, i
   const int orig_w = bvh->width, orig_leaf = bvh->leaf_size;
   bool first = true;
   for (int w : {2, 4, 8}) {
-    static const int kLeaves[3] = {1, 2, 4};
-    for (int li = 0; li < (w == 2 ? 1 : 3); ++li) {
+    static const int kLeaves[4] = {1, 2, 3, 4};
+    for (int li = 0; li < (w == 2 ? 1 : 4); ++li) {
       const int leaf = kLeaves[li];
       rc = flg_bvh_set_width(ctx, bvh, w, leaf);
       if (rc) goto done;

@@ -215,9 +215,11 @@ FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *ray
 FLG_API int flg_trace_closest_noalloc(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n,
                                       flg_hits *out);
 
-/* Sweeps node width (2/4/8), stack depth (32/64), persistent kernel on/off
- * with refill thresholds and ray sorting on the given workload, keeps the
- * fastest in *best and writes a JSON record (NUL-terminated) to json_out. */
+/* Sweeps node width (2/4/8) with leaf ranges of 1/2/3/4 triangles, stack
+ * depth (32/64), persistent kernel on/off with refill thresholds and ray
+ * sorting on the given workload; leaves the handle laid out at the fastest
+ * width and leaf size, returns the fastest options in *best and writes a JSON
+ * record (NUL-terminated) to json_out. */
 FLG_API int flg_autotune_trace(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n,
                                flg_trace_opts *best, int32_t *best_node_width, char *json_out,
                                size_t json_len);
