@@ -198,7 +198,9 @@ __device__ __forceinline__ int queue_slot(bool want, int32_t *counter) {
 // estimation toward one light triangle (Lambertian or Henyey-Greenstein
 // factor; the shadow ray's transmittance is applied in k_pt_shadow); the
 // continuation ray (cosine-weighted bounce or HGSampleP).
-__global__ void __launch_bounds__(256)
+// 4 CTAs per SM (64 registers, no spills; 74 without the bound): +1.3 % on a
+// 1080p / 16-spp render of a 1.3 M-triangle mesh.
+__global__ void __launch_bounds__(256, 4)
     k_pt_shade(PtScene S, Halton H, int s0, int depth, int64_t n_in, PtQueues Q, int qa, const int32_t *__restrict__ prim,
                const float *__restrict__ th, const float *__restrict__ uh, const float *__restrict__ vh) {
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
