@@ -135,6 +135,7 @@ struct PtQueues {
   float *rx[2][6];           // ray queues A/B: ox oy oz dx dy dz
   int32_t *path[2];          // queue slot -> path index
   float *sx[7];              // shadow queue: ox oy oz dx dy dz tmax
+  float *rsx[6];             // the same segments traced from the far end back: ox oy oz dx dy dz
   float *scontrib;           // 3 per shadow slot
   int32_t *spath;            // path of a shadow slot
   float *beta;               // 3 per path
@@ -341,6 +342,14 @@ __global__ void __launch_bounds__(256, 4)
     Q.sx[0][ss] = so.x; Q.sx[1][ss] = so.y; Q.sx[2][ss] = so.z;
     Q.sx[3][ss] = sd.x; Q.sx[4][ss] = sd.y; Q.sx[5][ss] = sd.z;
     Q.sx[6][ss] = smax;
+    // Occlusion is traced from the light end: on a closed surface the
+    // segments from the far side cross the hollow interior, where boxes of
+    // large surface patches overlap the ray without holding an occluder, but
+    // from the light the near side of the surface is found at once.  The
+    // segment is the same: [so, so + smax sd] from its far end, with the
+    // surface's own triangle (256 ulps behind so) still excluded.
+    Q.rsx[0][ss] = so.x + sd.x * smax; Q.rsx[1][ss] = so.y + sd.y * smax; Q.rsx[2][ss] = so.z + sd.z * smax;
+    Q.rsx[3][ss] = -sd.x; Q.rsx[4][ss] = -sd.y; Q.rsx[5][ss] = -sd.z;
     Q.scontrib[3 * ss] = contrib.x;
     Q.scontrib[3 * ss + 1] = contrib.y;
     Q.scontrib[3 * ss + 2] = contrib.z;
@@ -506,11 +515,11 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
   // so every bounce's trace launches fill the GPU.
   const int64_t kmax = std::max<int64_t>(1, std::min<int64_t>(spp, ((int64_t)1 << 25) / n));
   const int64_t np = kmax * n;  // path slots
-  // Buffers (per path slot): 2 x 6 ray arrays, 2 path maps, 7 shadow arrays
-  // + 3 contrib + path, beta 3, radiance 3, cnt, hits 4, occluded; cnt_end per
+  // Buffers (per path slot): 2 x 6 ray arrays, 2 path maps, 7 + 6 shadow
+  // arrays + 3 contrib + path, beta 3, radiance 3, cnt, hits 4, occluded; cnt_end per
   // pixel; counters.  Each sub-buffer is rounded up to 256 bytes.
   const size_t fl = sizeof(float) * np;
-  const size_t need = fl * (12 + 2 + 7 + 3 + 1 + 3 + 3 + 1 + 4) + sizeof(int32_t) * n + np + 64 + 32 * 256;
+  const size_t need = fl * (12 + 2 + 7 + 6 + 3 + 1 + 3 + 3 + 1 + 4) + sizeof(int32_t) * n + np + 64 + 38 * 256;
   if (ctx->pt_bytes < need) {
     cudaFree(ctx->pt_buf);
     ctx->pt_buf = nullptr;
@@ -531,6 +540,7 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
   Q.path[0] = (int32_t *)take(fl);
   Q.path[1] = (int32_t *)take(fl);
   for (int k = 0; k < 7; ++k) Q.sx[k] = (float *)take(fl);
+  for (int k = 0; k < 6; ++k) Q.rsx[k] = (float *)take(fl);
   Q.scontrib = (float *)take(3 * fl);
   Q.spath = (int32_t *)take(fl);
   Q.beta = (float *)take(3 * fl);
@@ -568,7 +578,7 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
       FLG_CUDA(ctx, cudaMemcpyAsync(counts, Q.counts, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
       FLG_CUDA(ctx, cudaStreamSynchronize(st));
       if (counts[1] > 0) {
-        flg_rays sr{Q.sx[0], Q.sx[1], Q.sx[2], Q.sx[3], Q.sx[4], Q.sx[5], nullptr, Q.sx[6], 1e-30f, 0.0f};
+        flg_rays sr{Q.rsx[0], Q.rsx[1], Q.rsx[2], Q.rsx[3], Q.rsx[4], Q.rsx[5], nullptr, Q.sx[6], 1e-30f, 0.0f};
         rc = trace_enqueue(ctx, st, 0, bvh, &sr, counts[1], opts, nullptr, 1, nullptr, occ);
         if (rc) return rc;
         n_shadow += counts[1];
