@@ -296,8 +296,9 @@ __device__ __forceinline__ dfl df_div(dfl x, dfl y) {
 // hit/miss and which triangle is closest; this makes the reported t, u, v
 // accurate to about an ulp even for grazing rays, where the fp32 quotients
 // lose digits.  Edges are formed exactly (e0 = c - a, e1 = a - b as
-// float-float).  Leaves the inputs unchanged when N.D is zero.
-__device__ __forceinline__ void refine_tuv(float3 a, float3 b, float3 c, float3 O, float3 D, float &t, float &u,
+// float-float).  Returns false, leaving the inputs unchanged, when N.D is
+// zero.
+__device__ __forceinline__ bool refine_tuv(float3 a, float3 b, float3 c, float3 O, float3 D, float &t, float &u,
                                            float &v) {
   const dfl e0x = two_sum(c.x, -a.x), e0y = two_sum(c.y, -a.y), e0z = two_sum(c.z, -a.z);
   const dfl e1x = two_sum(a.x, -b.x), e1y = two_sum(a.y, -b.y), e1z = two_sum(a.z, -b.z);
@@ -318,13 +319,14 @@ __device__ __forceinline__ void refine_tuv(float3 a, float3 b, float3 c, float3 
   const dfl Ny = df_sub(df_mul(e0z, e1x), df_mul(e0x, e1z));
   const dfl Nz = df_sub(df_mul(e0x, e1y), df_mul(e0y, e1x));
   const dfl den = df_add(df_add(df_mulf(Nx, D.x), df_mulf(Ny, D.y)), df_mulf(Nz, D.z));
-  if (den.hi == 0.0f) return;
+  if (den.hi == 0.0f) return false;
   const dfl num = df_add(df_add(df_mul(v0x, Nx), df_mul(v0y, Ny)), df_mul(v0z, Nz));
   const dfl S = dfl{2.0f * den.hi, 2.0f * den.lo};
   const dfl tt = df_div(num, den), uu = df_div(U, S), vv = df_div(V, S);
   t = tt.hi + tt.lo;
   u = uu.hi + uu.lo;
   v = vv.hi + vv.lo;
+  return true;
 }
 
 // Accept a candidate t for closest hit: tmin <= t, and t < best (or t == best

@@ -147,7 +147,7 @@ __device__ __forceinline__ void write_result(const Out &O, int64_t i, bool any, 
 // barycentrics from the Pluecker quantities, then t, u, v recomputed in
 // float-float and rounded once (refine_tuv); the sorted position becomes
 // the caller's triangle id.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
     k_trace_finish(RaySoA R, int64_t n, Out O, const TriRec *__restrict__ tris) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int32_t g = O.prim[i];
@@ -157,9 +157,12 @@ __global__ void __launch_bounds__(256)
     const float4 *p = (const float4 *)(tris + g);
     const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
     const float3 pa = make_float3(a.x, a.y, a.z), pb = make_float3(b.x, b.y, b.z), pc = make_float3(c.x, c.y, c.z);
-    float best = O.t[i], u = 0.0f, v = 0.0f, tf;
-    pluecker(pa, pb, pc, o, d, tf, u, v);
-    refine_tuv(pa, pb, pc, o, d, best, u, v);
+    float best = O.t[i], u = 0.0f, v = 0.0f;
+    if (!refine_tuv(pa, pb, pc, o, d, best, u, v)) {
+      // N.D == 0: the fp32 barycentrics of the test stand (t stays the test's)
+      float tf;
+      pluecker(pa, pb, pc, o, d, tf, u, v);
+    }
     O.prim[i] = __float_as_int(a.w);
     O.t[i] = best;
     O.u[i] = u;
