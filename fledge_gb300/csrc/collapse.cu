@@ -1,7 +1,9 @@
 // collapse.cu — re-lays out a built Karras BVH2 as 4- or 8-wide nodes for
-// traversal.  Top-down, one launch per level: each queued BVH2 node becomes a
-// wide node whose children are found by repeatedly opening the child with
-// the largest surface area (Wald, Benthin, Boulos 2008 style collapsing).
+// traversal.  Top-down, level by level (one cooperative launch with a grid
+// barrier between levels; one launch per level under stream capture): each
+// queued BVH2 node becomes a wide node whose children are found by
+// repeatedly opening the child with the largest surface area (Wald, Benthin,
+// Boulos 2008 style collapsing).
 // A BVH2 subtree covers a contiguous run of sorted triangles, so any subtree
 // with at most leaf_size triangles becomes a leaf range [first, first+count).
 // The Karras topology itself (the parity object) is unchanged.
