@@ -333,27 +333,32 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             h.destroy()
         del handles
 
-    # ---- high-quality builder (PLOC) on the same scenes and rays ----
+    # ---- high-quality builders (PLOC, binned SAH) on the same scenes and rays ----
     log('plain path done' if plain else 'plain skipped')
-    hq = None
+    hq = sah = None
     if not args.skip_hq:
-        hb = F.BatchedRadixBVHBuilder(mesh, offs, ctx, node_width=width, leaf_size=leaf, builder="ploc")
-        hb.build()
-        hb.intersect_batched(rays, roffs, out=hits, **topts)  # warm-up
-        torch.cuda.synchronize()
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-        ev[0].record(stream)
-        hb.build()
-        ev[1].record(stream)
-        hb.intersect_batched(rays, roffs, out=hits, **topts)
-        ev[2].record(stream)
-        torch.cuda.synchronize()
-        hb_ms, ht_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
-        hq = {"builder": "ploc (radius 16)", "build_ms": round(hb_ms, 3), "trace_ms": round(ht_ms, 2),
-              "mrays_s": round(n_rays / (ht_ms * 1e-3) / 1e6, 1),
-              "trace_speedup_vs_lbvh": round(statistics.median(trace_ms) / ht_ms, 3),
-              "step_ms": round(hb_ms + ht_ms, 2)}
-        hb.destroy()
+        res = {}
+        for name in ("ploc", "sah"):
+            hb = F.BatchedRadixBVHBuilder(mesh, offs, ctx, node_width=width, leaf_size=leaf, builder=name)
+            hb.build()
+            hb.intersect_batched(rays, roffs, out=hits, **topts)  # warm-up
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            ev[0].record(stream)
+            hb.build()
+            ev[1].record(stream)
+            hb.intersect_batched(rays, roffs, out=hits, **topts)
+            ev[2].record(stream)
+            torch.cuda.synchronize()
+            hb_ms, ht_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+            res[name] = {"builder": "ploc (radius 16)" if name == "ploc" else "binned SAH (16 buckets, reference rule)",
+                         "build_ms": round(hb_ms, 3), "trace_ms": round(ht_ms, 2),
+                         "mrays_s": round(n_rays / (ht_ms * 1e-3) / 1e6, 1),
+                         "trace_speedup_vs_lbvh": round(statistics.median(trace_ms) / ht_ms, 3),
+                         "step_ms": round(hb_ms + ht_ms, 2)}
+            hb.destroy()
+            log(f'{name} builder done')
+        hq, sah = res["ploc"], res["sah"]
 
     # ---- e2e: host (pinned) inputs, copies inside the timed region ----
     e2e = None
@@ -400,7 +405,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                            "parallelism": f"replicas x{world}"},
                 "build_ms": round(b_ms, 3), "trace_ms": round(tr_ms, 3), "hit_rate": round(hit_rate, 4),
                 "build_roofline": build_roof, "roofline": roof, "plain": plain, "volume": vol,
-                "hq_builder": hq, "config0": c0, "config1": c1, "config1_volume": c1v, "config4": c4,
+                "hq_builder": hq, "sah_builder": sah, "config0": c0, "config1": c1, "config1_volume": c1v, "config4": c4,
                 "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu, "gpu_launches": int(launches),
                 "gpu_launches_total": int(total_launches)}
         print(json.dumps(line), flush=True)
@@ -767,7 +772,7 @@ def main() -> None:
     ap.add_argument("--skip-c4", action="store_true")
     ap.add_argument("--skip-c1", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--skip-hq", action="store_true", help="skip the PLOC-builder comparison")
+    ap.add_argument("--skip-hq", action="store_true", help="skip the PLOC and SAH builder comparisons")
     ap.add_argument("--scenes", type=int, default=256, help="diagnostics only: first N scenes")
     ap.add_argument("--verbose", action="store_true", help="progress on stderr")
     args = ap.parse_args()

@@ -144,8 +144,9 @@ def _trace_opts(stack_depth=0, block_threads=0, persistent=0, refill_lanes=0, ra
 
 
 def _builder_id(name: str) -> int:
-    """'lbvh' (the Karras radix tree) or 'ploc' (locally-ordered clustering)."""
-    ids = {"lbvh": _lib.FLG_BUILDER_LBVH, "ploc": _lib.FLG_BUILDER_PLOC}
+    """'lbvh' (the Karras radix tree), 'ploc' (locally-ordered clustering) or
+    'sah' (BasicBVHBuilder's binned-SAH build)."""
+    ids = {"lbvh": _lib.FLG_BUILDER_LBVH, "ploc": _lib.FLG_BUILDER_PLOC, "sah": _lib.FLG_BUILDER_SAH}
     if name not in ids:
         raise ValueError(f"builder must be one of {sorted(ids)}")
     return ids[name]

@@ -439,6 +439,16 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
   const unsigned fill_grid = grid_for(b->n_scenes, 128);
   k_init_boxes<<<fill_grid, 128, 0, st>>>(b->d_scene_box, b->n_scenes);
   FLG_LAUNCH_CHECK(ctx, "k_init_boxes");
+  if (b->builder == FLG_BUILDER_SAH) {
+    // Top-down from the scene bounds; no Morton codes or sort.
+    k_scene_bounds<<<grid_for(n, kBoundsChunk), kBoundsThreads, 0, st>>>(b->pos, b->idx, n, b->d_tri_off,
+                                                                       b->n_scenes, b->d_scene_box);
+    FLG_LAUNCH_CHECK(ctx, "k_scene_bounds");
+    int rc = sah_build(ctx, b);
+    if (rc) return rc;
+    if (b->width > 2) return collapse_enqueue(ctx, b, b->width, b->leaf_size);
+    return FLG_OK;
+  }
   if (b->d_tile_start) {
     FLG_CUDA(ctx, cudaMemsetAsync(b->d_shist, 0, sizeof(uint32_t) * 4 * 256 * (size_t)b->n_scenes, st));
   } else {
@@ -520,8 +530,8 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   if (width != 2 && width != 4 && width != 8) return set_error(ctx, FLG_ERR_ARG, "node_width must be 2, 4 or 8");
   if (leaf_size < 1 || leaf_size > 8) return set_error(ctx, FLG_ERR_ARG, "leaf_size must be in [1, 8]");
   const int builder = opts ? opts->builder : FLG_BUILDER_LBVH;
-  if (builder != FLG_BUILDER_LBVH && builder != FLG_BUILDER_PLOC)
-    return set_error(ctx, FLG_ERR_ARG, "builder must be FLG_BUILDER_LBVH or FLG_BUILDER_PLOC");
+  if (builder != FLG_BUILDER_LBVH && builder != FLG_BUILDER_PLOC && builder != FLG_BUILDER_SAH)
+    return set_error(ctx, FLG_ERR_ARG, "builder must be FLG_BUILDER_LBVH, FLG_BUILDER_PLOC or FLG_BUILDER_SAH");
 
   flg_bvh b = new flg_bvh_t();
   b->ctx = ctx;
@@ -589,6 +599,7 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   A(&b->d_lookback, 256 * (size_t)b->n_tiles * b->n_passes);
   A(&b->d_tile_ctr, b->n_passes);
   if (rc == FLG_OK && builder == FLG_BUILDER_PLOC) rc = ploc_reserve(b);
+  if (rc == FLG_OK && builder == FLG_BUILDER_SAH) rc = sah_reserve(b);
   if (rc) {
     flg_bvh_destroy(b);
     return rc;
@@ -704,8 +715,8 @@ FLG_API int flg_bvh_info_get(flg_bvh bvh, flg_bvh_info *out) {
 FLG_API int flg_bvh_download(flg_bvh bvh, int32_t scene, flg_bvh_topology *t) {
   if (!bvh || !t) return FLG_ERR_ARG;
   flg_ctx ctx = bvh->ctx;
-  if (bvh->builder != FLG_BUILDER_LBVH)
-    return set_error(ctx, FLG_ERR_UNSUPPORTED, "only LBVH handles keep the Karras arrays");
+  if (bvh->builder == FLG_BUILDER_PLOC)
+    return set_error(ctx, FLG_ERR_UNSUPPORTED, "PLOC handles keep no Karras-numbered node records");
   if (scene < 0 || scene >= bvh->n_scenes) return set_error(ctx, FLG_ERR_ARG, "scene out of range");
   cudaStream_t st = ctx->stream;
   const int64_t toff = bvh->tri_off_h[scene];

@@ -136,6 +136,18 @@ struct flg_bvh_t {
   int32_t *d_newpos = nullptr, *d_lcount = nullptr;
   int2 *d_lq[2] = {nullptr, nullptr};
   int32_t n_nonempty = 0;
+  // SAH builds (builder == FLG_BUILDER_SAH): per position, ping-pong
+  // triangle boxes (2 float4), centroids (xyz + original index) and the
+  // level-list index of the position's node; per level, the node list and
+  // its 16 bucket records (8 words each); finished ranges, flag scan,
+  // counters and the roots' list indices.
+  int64_t sah_cap = 0, sah_fin_cap = 0;
+  float4 *d_sbox[2] = {nullptr, nullptr}, *d_scen[2] = {nullptr, nullptr};
+  int32_t *d_sseg[2] = {nullptr, nullptr};
+  void *d_slist[2] = {nullptr, nullptr};
+  uint32_t *d_sbins[2] = {nullptr, nullptr};
+  int4 *d_sfin = nullptr;
+  int32_t *d_sflag = nullptr, *d_sscan = nullptr, *d_ssum = nullptr, *d_sctr = nullptr, *d_sroot = nullptr;
 };
 
 struct flg_grid_t {
@@ -212,6 +224,17 @@ int sort_pairs_enqueue(flg_ctx ctx, cudaStream_t st, int64_t n, int passes, uint
                        uint32_t *const vals[2], uint32_t *hist, uint32_t *lookback, uint32_t *tile_ctr);
 int ploc_reserve(flg_bvh b);
 int ploc_build(flg_ctx ctx, flg_bvh b);
+int sah_reserve(flg_bvh b);
+int sah_build(flg_ctx ctx, flg_bvh b);
+// Exclusive scan of int32 flags (ploc.cu): per-tile scans and tile sums
+// (kFlagScanThreads threads, kFlagScanTile flags per tile), then a one-CTA
+// (1024 threads) exclusive scan of the tile sums that also writes the total.
+constexpr int kFlagScanThreads = 256;
+constexpr int kFlagScanTile = 4096;
+#ifdef __CUDACC__
+__global__ void k_scan_tiles(const int32_t *in, int n, int32_t *out, int32_t *tsum);
+__global__ void k_scan_sums(int32_t *tsum, int nt, int32_t *total_out);
+#endif
 int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_rays *rays, int64_t n,
                   const flg_trace_opts *opts, const int64_t *ray_off_dev, int n_scenes, flg_hits *hits,
                   uint8_t *occ);

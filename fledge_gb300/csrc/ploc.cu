@@ -36,6 +36,7 @@ constexpr int kPlocThreads = 256;
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
+static_assert(kScanThreads == kFlagScanThreads && kScanTile == kFlagScanTile, "flag scan shape");
 
 __device__ __forceinline__ float merged_half_area(float4 alo, float4 ahi, float4 blo, float4 bhi) {
   const float dx = fmaxf(ahi.x, bhi.x) - fminf(alo.x, blo.x);

@@ -75,18 +75,27 @@ typedef struct flg_build_opts {
   int32_t node_width;     /* traversal layout: 2, 4 or 8 (0 = 4) */
   int32_t leaf_size;      /* wide layouts: max triangles per leaf range (0 = 1) */
   int32_t keep_topology;  /* unused: flg_bvh_download derives the Karras arrays from the nodes */
-  int32_t builder;        /* FLG_BUILDER_LBVH (0, the Karras radix tree) or FLG_BUILDER_PLOC */
+  int32_t builder;        /* FLG_BUILDER_LBVH (0, the Karras radix tree), FLG_BUILDER_PLOC or
+                             FLG_BUILDER_SAH */
 } flg_build_opts;
 
-/* Tree builders.  FLG_BUILDER_PLOC is the high-quality alternative to the
- * LBVH (the role of BasicBVHBuilder's SAH build, src/experimental/
- * base_bvh.cpp:33-188): parallel locally-ordered clustering over the same
- * Morton order (Meister & Bittner 2018), i.e. repeated merging of mutual
- * nearest clusters within a window of the sorted sequence, by the surface
- * area of the merged box.  Its builds synchronise with the host once per
- * clustering iteration (not capturable), and its handles keep no Karras
- * arrays (flg_bvh_download returns FLG_ERR_UNSUPPORTED). */
-enum { FLG_BUILDER_LBVH = 0, FLG_BUILDER_PLOC = 1 };
+/* Tree builders.  FLG_BUILDER_PLOC is a high-quality alternative to the
+ * LBVH: parallel locally-ordered clustering over the same Morton order
+ * (Meister & Bittner 2018), i.e. repeated merging of mutual nearest clusters
+ * within a window of the sorted sequence, by the surface area of the merged
+ * box.  Its builds synchronise with the host once per clustering iteration
+ * (not capturable), and its handles keep no Karras arrays (flg_bvh_download
+ * returns FLG_ERR_UNSUPPORTED).
+ * FLG_BUILDER_SAH is BasicBVHBuilder's binned-SAH build
+ * (src/experimental/base_bvh.cpp:33-173 with EBVHPartitionMethod::ESAH at
+ * every node): top down, 16 buckets of triangle centroids along axis
+ * depth % 3, cost 1/8 + (SA_L n_L + SA_R n_R) / SA, leaves at <= 8
+ * triangles, depth 26 or no split cheaper than the leaf; stable partitions,
+ * bucket indices clamped to [0, 15], and leaves of k > 1 triangles stored as
+ * balanced binary subtrees.  Nodes are numbered as in the Karras tree, so
+ * flg_bvh_download returns its topology (morton is not filled).  One host
+ * synchronisation per tree level (not capturable). */
+enum { FLG_BUILDER_LBVH = 0, FLG_BUILDER_PLOC = 1, FLG_BUILDER_SAH = 2 };
 
 typedef struct flg_trace_opts {
   int32_t stack_depth;    /* 32 or 64 (0 = 64); overflowing rays are retried deeper */

@@ -73,7 +73,7 @@ struct DeviceMesh {
 
 class RadixBVHBuilder {
  public:
-  // builder: FLG_BUILDER_LBVH (the Karras radix tree) or FLG_BUILDER_PLOC.
+  // builder: FLG_BUILDER_LBVH (the Karras radix tree), FLG_BUILDER_PLOC or FLG_BUILDER_SAH.
   RadixBVHBuilder(Context &ctx, const DeviceMesh &mesh, int node_width = 4, int leaf_size = 1,
                   int builder = FLG_BUILDER_LBVH)
       : ctx_(ctx), mesh_(mesh), opts_{node_width, leaf_size, 1, builder} {}

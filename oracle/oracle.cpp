@@ -816,6 +816,145 @@ ORC_API void orc_refit(const float *pos, const int32_t *idx, int64_t n64, const 
     }
 }
 
+// Binned-SAH build: BasicBVHBuilder::recursiveBuilder with
+// EBVHPartitionMethod::ESAH at every node (src/experimental/base_bvh.cpp:33-173),
+// written out as a tree in the Karras arrays' form:
+//   * leaf when n <= 8 or depth >= 26 (:44); otherwise 16 buckets of the
+//     centroids (a + b + c) / 3 (base_bvh.hpp:86-87) along axis depth % 3
+//     (:53, :113-114), costs 1/8 + (SA_L n_L + SA_R n_R) / SA for the splits
+//     after buckets 1..14 (:138-152, SA as base_bvh.hpp:58-63, the 1/8 added
+//     in double), the first minimum taken, a split only below the leaf cost n
+//     (:154-165);
+//   * bucket indices outside [0, 15] are clamped, NaN to 0 (the reference
+//     indexes out of bounds there), and the partition is stable (std::partition
+//     leaves the order unspecified);
+//   * a leaf of k > 1 triangles is stored as a balanced binary subtree (left
+//     part k / 2); internal nodes are numbered as Karras numbers them (root 0,
+//     a left child by its last position, a right child by its first).
+namespace {
+struct SahRec {
+  Bound b;
+  float c[3];
+  int32_t orig;
+};
+
+inline float sah_area(const Bound &b) {
+  float ex = b.hi[0] - b.lo[0], ey = b.hi[1] - b.lo[1], ez = b.hi[2] - b.lo[2];
+  return 2 * (ex * ey + ex * ez + ey * ez);
+}
+
+inline int sah_bucket(float c, float lo, float hi) {
+  float f = std::floor(((c - lo) / (hi - lo)) * 16);
+  return f >= 0.0f ? (f < 16.0f ? (int)f : 15) : 0;
+}
+
+struct SahOut {
+  std::vector<SahRec> r;
+  int32_t *split;
+  uint8_t *leaf;
+  int32_t *range_j, *parent, *leaf_parent;
+  float *nb;
+
+  Bound range_bound(int64_t f, int64_t cnt) const {
+    Bound b;
+    for (int64_t i = f; i < f + cnt; ++i) b.merge(r[i].b);
+    return b;
+  }
+
+  void node(int64_t f, int64_t cnt, int depth, bool sah, int64_t slot) {
+    const Bound B = range_bound(f, cnt);
+    int64_t h = -1;
+    Bound lb, rb;
+    if (sah && !(cnt <= 8 || depth >= 26)) {
+      const int dim = depth % 3;
+      Bound bb[16], pre[16], suf[16];
+      int64_t bn[16] = {0}, pn[16], sn[16];
+      for (int64_t i = f; i < f + cnt; ++i) {
+        int b = sah_bucket(r[i].c[dim], B.lo[dim], B.hi[dim]);
+        bb[b].merge(r[i].b);
+        ++bn[b];
+      }
+      pre[0] = bb[0];
+      pn[0] = bn[0];
+      for (int i = 1; i < 16; ++i) {
+        pre[i] = pre[i - 1];
+        pre[i].merge(bb[i]);
+        pn[i] = pn[i - 1] + bn[i];
+      }
+      suf[15] = bb[15];
+      sn[15] = bn[15];
+      for (int i = 14; i >= 0; --i) {
+        suf[i] = suf[i + 1];
+        suf[i].merge(bb[i]);
+        sn[i] = sn[i + 1] + bn[i];
+      }
+      float min_cost = FLT_MAX;
+      int min_i = 0;
+      for (int i = 1; i < 15; ++i) {
+        float q = (sah_area(pre[i]) * (float)pn[i] + sah_area(suf[i + 1]) * (float)sn[i + 1]) / sah_area(B);
+        float cost = (float)(1.0 / 8 + (double)q);
+        if (cost < min_cost) {
+          min_cost = cost;
+          min_i = i;
+        }
+      }
+      if (min_cost < (float)cnt) {
+        std::stable_partition(r.begin() + f, r.begin() + f + cnt, [&](const SahRec &t) {
+          return sah_bucket(t.c[dim], B.lo[dim], B.hi[dim]) <= min_i;
+        });
+        h = pn[min_i];
+        lb = pre[min_i];
+        rb = suf[min_i + 1];
+      }
+    }
+    const bool child_sah = sah && h >= 0;
+    if (h < 0) {
+      h = cnt / 2;
+      lb = range_bound(f, h);
+      rb = range_bound(f + h, cnt - h);
+    }
+    const int64_t last = f + cnt - 1, m = f + h;
+    split[slot] = (int32_t)(m - 1);
+    leaf[slot] = (uint8_t)((h == 1 ? 1 : 0) | (cnt - h == 1 ? 2 : 0));
+    range_j[slot] = (int32_t)(slot == f ? last : f);
+    for (int k = 0; k < 3; ++k) {
+      nb[6 * slot + k] = std::min(lb.lo[k], rb.lo[k]);
+      nb[6 * slot + 3 + k] = std::max(lb.hi[k], rb.hi[k]);
+    }
+    if (h == 1) leaf_parent[f] = (int32_t)slot; else parent[m - 1] = (int32_t)slot;
+    if (cnt - h == 1) leaf_parent[m] = (int32_t)slot; else parent[m] = (int32_t)slot;
+    if (h >= 2) node(f, h, depth + 1, child_sah, m - 1);
+    if (cnt - h >= 2) node(m, cnt - h, depth + 1, child_sah, m);
+  }
+};
+}  // namespace
+
+ORC_API void orc_build_sah(const float *pos, const int32_t *idx, int64_t n, int32_t *perm, int32_t *split,
+                           uint8_t *leaf, int32_t *range_j, int32_t *parent, int32_t *leaf_parent, float *nb) {
+  Mesh M{pos, idx, n};
+  SahOut S;
+  S.r.resize((size_t)n);
+  for (int64_t i = 0; i < n; ++i) {
+    const float *a = M.v(i, 0), *b = M.v(i, 1), *c = M.v(i, 2);
+    S.r[i].b = M.bound(i);
+    for (int k = 0; k < 3; ++k) S.r[i].c[k] = (a[k] + b[k] + c[k]) / 3;
+    S.r[i].orig = (int32_t)i;
+  }
+  S.split = split;
+  S.leaf = leaf;
+  S.range_j = range_j;
+  S.parent = parent;
+  S.leaf_parent = leaf_parent;
+  S.nb = nb;
+  if (n >= 2) {
+    parent[0] = 0;
+    S.node(0, n, 0, true, 0);
+  } else if (n == 1) {
+    leaf_parent[0] = -1;
+  }
+  for (int64_t i = 0; i < n; ++i) perm[i] = S.r[i].orig;
+}
+
 // Closest hit over a tree built by the functions above (recursiveIntersect).
 // rays: 8 SoA arrays of n floats (ox oy oz dx dy dz tmin tmax).  out: prim
 // (-1 = miss), t, u, v.

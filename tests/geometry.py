@@ -89,3 +89,14 @@ def value_noise_grid(res, rng, scale=4.0):
     g = g[:, i0] * (1 - f)[None, :, None] + g[:, i0 + 1] * f[None, :, None]
     g = g[:, :, i0] * (1 - f)[None, None, :] + g[:, :, i0 + 1] * f[None, None, :]
     return (scale * g).astype(np.float32)
+
+
+def geometric_clusters(n_scales, per_scale, rng):
+    """Clusters of per_scale small triangles at (2^-k, 2^-k, 2^-k), k < n_scales:
+    a top-down split peels off one scale at a time, so trees reach any depth."""
+    out = []
+    for k in range(n_scales):
+        c = np.float32(2.0 ** -k)
+        tri = c + (rng.uniform(-1.0, 1.0, (per_scale, 3, 3)) * (0.02 * c)).astype(np.float32)
+        out.append(tri.astype(np.float32))
+    return np.concatenate(out).reshape(-1, 3)
