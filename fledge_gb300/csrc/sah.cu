@@ -37,7 +37,7 @@
 // SAH rule is the one the reference writes out for a high-quality build.
 //
 // One level: k_sah_bin (bucket boxes and counts of every node: shared-memory
-// bins when a 2048-position chunk lies inside one node, global atomics
+// bins when a 2048-position chunk holds at most 32 nodes, global atomics
 // otherwise), k_sah_split (one thread per node: the rule above, the node
 // record, children queued for the next level or finished), k_sah_flags and
 // the flag scan (stable partition ranks), k_sah_scatter (records to their new
@@ -202,36 +202,78 @@ __device__ __forceinline__ int sah_side_bucket(const SahNode &N, int64_t p, cons
   return sah_bucket(comp(c, axis), comp(N.lo, axis), comp(N.hi, axis));
 }
 
-// Bucket boxes and counts.  A CTA takes chunks of 2048 positions; a chunk
-// inside one node (its first and last position in the same node: nodes are
-// contiguous ranges) is binned in shared memory and flushed with one atomic
-// per word, others go to the global bins directly.
+// Bucket boxes and counts.  A CTA takes chunks of 2048 positions and splits
+// each into runs of equal list index (nodes are contiguous position ranges,
+// so a run is the part of one node inside the chunk).  With at most 32 runs
+// the chunk is binned in shared memory and flushed with one atomic per
+// non-empty bucket word; otherwise (nodes of a few dozen triangles) every
+// position goes to the global bins directly.
+constexpr int kSahRuns = 32;
 __global__ void __launch_bounds__(kSahBinThreads)
     k_sah_bin(const float4 *__restrict__ box, const float4 *__restrict__ cen, const int32_t *__restrict__ seg,
               int64_t n, const SahNode *__restrict__ list, uint32_t *bins, int axis) {
-  __shared__ uint32_t s_bins[kSahBuckets * kSahBinWords];
+  __shared__ uint32_t s_bins[kSahRuns * kSahBuckets * kSahBinWords];
+  __shared__ uint8_t s_run[kSahChunk];
+  __shared__ int32_t s_rseg[kSahRuns];
+  __shared__ int32_t s_warp[kSahBinThreads / 32];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   for (int64_t c0 = (int64_t)blockIdx.x * kSahChunk; c0 < n; c0 += (int64_t)gridDim.x * kSahChunk) {
     const int64_t c1 = min(c0 + (int64_t)kSahChunk, n) - 1;
-    const int sa = seg[c0], sb = seg[c1];
-    const bool local = sa >= 0 && sa == sb;
-    if (local) {
-      if (threadIdx.x < kSahBuckets * kSahBinWords) {
-        const int w = threadIdx.x % kSahBinWords;
-        s_bins[threadIdx.x] = w < 3 ? fkey(FLT_MAX) : w < 6 ? fkey(-FLT_MAX) : 0u;
-      }
-      __syncthreads();
+    // Run starts over positions c0 + 8t .. c0 + 8t + 7, then a block scan.
+    int sv[kSahBinItems];
+    int starts = 0;
+    uint32_t smask = 0;
+#pragma unroll
+    for (int j = 0; j < kSahBinItems; ++j) {
+      const int64_t p = c0 + (int64_t)kSahBinItems * t + j;
+      sv[j] = p <= c1 ? seg[p] : -1;
+      const bool st = p <= c1 && (p == c0 || sv[j] != (j > 0 ? sv[j - 1] : seg[p - 1]));
+      starts += st ? 1 : 0;
+      smask |= st ? (1u << j) : 0u;
     }
-    SahNode N;
-    if (local) N = list[sa];
+    int incl = starts;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    int base = 0, runs = 0;
+#pragma unroll
+    for (int w = 0; w < kSahBinThreads / 32; ++w) {
+      base += w < warp ? s_warp[w] : 0;
+      runs += s_warp[w];
+    }
+    const bool local = runs <= kSahRuns;
+    if (local) {
+      int r = base + incl - starts - 1;
+#pragma unroll
+      for (int j = 0; j < kSahBinItems; ++j) {
+        const int64_t p = c0 + (int64_t)kSahBinItems * t + j;
+        if (p > c1) break;
+        if (smask & (1u << j)) {
+          ++r;
+          s_rseg[r] = sv[j];
+        }
+        s_run[kSahBinItems * t + j] = (uint8_t)r;
+      }
+      for (int w = t; w < runs * kSahBuckets * kSahBinWords; w += kSahBinThreads) {
+        const int k = w % kSahBinWords;
+        s_bins[w] = k < 3 ? fkey(FLT_MAX) : k < 6 ? fkey(-FLT_MAX) : 0u;
+      }
+    }
+    __syncthreads();
     for (int k = 0; k < kSahBinItems; ++k) {
-      const int64_t p = c0 + (int64_t)k * kSahBinThreads + threadIdx.x;
+      const int64_t p = c0 + (int64_t)k * kSahBinThreads + t;
       if (p > c1) break;
-      const int s = local ? sa : seg[p];
+      const int s = seg[p];
       if (s < 0) continue;
-      if (!local) N = list[s];
+      const SahNode N = list[s];
       const int b = sah_side_bucket(N, p, cen[p], axis);
       const float4 bl = box[2 * p], bh = box[2 * p + 1];
-      uint32_t *d = local ? s_bins + b * kSahBinWords : bins + ((int64_t)s * kSahBuckets + b) * kSahBinWords;
+      uint32_t *d = local ? s_bins + ((int)s_run[k * kSahBinThreads + t] * kSahBuckets + b) * kSahBinWords
+                          : bins + ((int64_t)s * kSahBuckets + b) * kSahBinWords;
       atomicMin(d + 0, fkey(bl.x));
       atomicMin(d + 1, fkey(bl.y));
       atomicMin(d + 2, fkey(bl.z));
@@ -242,18 +284,19 @@ __global__ void __launch_bounds__(kSahBinThreads)
     }
     if (local) {
       __syncthreads();
-      if (threadIdx.x < kSahBuckets * 7) {
-        const int b = threadIdx.x / 7, w = threadIdx.x % 7;
-        if (s_bins[b * kSahBinWords + 6] > 0) {
-          const uint32_t v = s_bins[b * kSahBinWords + w];
-          uint32_t *d = bins + ((int64_t)sa * kSahBuckets + b) * kSahBinWords + w;
-          if (w < 3) atomicMin(d, v);
-          else if (w < 6) atomicMax(d, v);
-          else atomicAdd(d, v);
+      for (int e = t; e < runs * kSahBuckets * 7; e += kSahBinThreads) {
+        const int r = e / (kSahBuckets * 7), b = (e / 7) % kSahBuckets, w = e % 7;
+        const int s = s_rseg[r];
+        const uint32_t *src = s_bins + (r * kSahBuckets + b) * kSahBinWords;
+        if (s >= 0 && src[6] > 0) {
+          uint32_t *d = bins + ((int64_t)s * kSahBuckets + b) * kSahBinWords + w;
+          if (w < 3) atomicMin(d, src[w]);
+          else if (w < 6) atomicMax(d, src[w]);
+          else atomicAdd(d, src[w]);
         }
       }
-      __syncthreads();
     }
+    __syncthreads();
   }
 }
 
