@@ -108,6 +108,18 @@ class ClockSampler:
 # CPU reference arm (the oracle restates the reference; run on all host cores)
 # ---------------------------------------------------------------------------
 
+def sah_cpu(O, scenes, n_tri_gpu: int, gpu_build_ms: float) -> dict:
+    """The oracle's binned-SAH build (one thread, recursive) on the largest
+    scene of the CPU sample, beside the GPU's batched SAH build rate."""
+    pos = max((p for p, _ in scenes), key=lambda p: p.shape[0])
+    n = pos.shape[0] // 3
+    t0 = time.perf_counter()
+    O.build_bvh_sah(pos)
+    dt = time.perf_counter() - t0
+    return {"cpu_mtris_s": round(n / dt / 1e6, 3), "gpu_mtris_s": round(n_tri_gpu / (gpu_build_ms * 1e-3) / 1e6, 1),
+            "cpu_sample": f"oracle SAH build of one {n}-triangle scene, 1 thread ({dt:.2f} s)"}
+
+
 def cpu_sample(max_tris: int = 1_500_000, rays_cap: int = 2_000_000):
     """Bounded sample of the headline workload for the CPU: the first scenes
     of the batch up to max_tris triangles, 64 rays per triangle capped at
@@ -391,6 +403,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         cpu = {"value": round(nr / dt / 1e6, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
                "sample": f"{len(scenes)} scenes, {ntri} triangles, {nr} rays: oracle build + closest hit "
                          f"({dt:.1f} s)"}
+        if sah is not None:
+            sah.update(sah_cpu(O, scenes, n_tri, sah["build_ms"]))
 
     total_launches = lib.flg_ctx_launch_count(ctx.h) - launches0
     if rank == 0:
