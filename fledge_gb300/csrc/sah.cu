@@ -1,7 +1,7 @@
 // sah.cu — binned-SAH top-down builder (FLG_BUILDER_SAH): the split rule of
 // BasicBVHBuilder::recursiveBuilder with EBVHPartitionMethod::ESAH
 // (src/experimental/base_bvh.cpp:33-173), applied to every node of every
-// scene, one tree level per round of launches.
+// scene, one tree level per sequence of launches.
 //
 // The rule at a node of n triangles at depth d (root 0):
 //   * a leaf when n <= 8 or d >= 26 (base_bvh.cpp:44);
