@@ -78,3 +78,18 @@ def test_product_path_never_imports_oracle():
             if f.endswith((".py", ".cu", ".cuh", ".h")):
                 src = open(os.path.join(dirpath, f)).read()
                 assert "oracle" not in src.replace("Oracle", "").lower() or f == "_build.py", f
+
+
+def test_builder_ids_match_header():
+    """FLG_BUILDER_* in include/flg.h, the ctypes constants and the Python
+    mirror's builder names agree; unknown names are rejected."""
+    import fledge_gb300 as F
+    import fledge_gb300._lib as L
+    text = open(HEADER).read()
+    enum = dict(re.findall(r"(FLG_BUILDER_\w+)\s*=\s*(\d+)", text))
+    assert enum == {"FLG_BUILDER_LBVH": "0", "FLG_BUILDER_PLOC": "1", "FLG_BUILDER_SAH": "2"}
+    for k, v in enum.items():
+        assert getattr(L, k) == int(v)
+    assert [F._builder_id(n) for n in ("lbvh", "ploc", "sah")] == [0, 1, 2]
+    with pytest.raises(ValueError):
+        F._builder_id("median")
