@@ -269,7 +269,7 @@ inline bool moller(V3 p0, V3 p1, V3 p2, V3 O, V3 D, Hit *h) {
   return true;
 }
 
-inline bool pluecker(V3 a, V3 b, V3 c, V3 O, V3 D, int mode, Hit *h) {
+inline bool pluecker(V3 a, V3 b, V3 c, V3 O, V3 D, int mode, Hit *h, V3 *ng_out = nullptr) {
   if (mode == MODE_MT) return moller(a, b, c, O, D, h);
   V3 v0 = sub(a, O), v1 = sub(b, O), v2 = sub(c, O);
   V3 e0 = sub(v2, v0), e1 = sub(v0, v1), e2 = sub(v1, v2);
@@ -297,6 +297,7 @@ inline bool pluecker(V3 a, V3 b, V3 c, V3 O, V3 D, int mode, Hit *h) {
   h->t = t;
   h->u = UVW != 0.0f ? U / UVW : 0.0f;
   h->v = UVW != 0.0f ? V / UVW : 0.0f;
+  if (ng_out) *ng_out = Ng;  // the normal the reference stores in BVHRayHit::hit_ng
   return true;
 }
 
@@ -1016,6 +1017,29 @@ ORC_API int orc_pluecker(const float *a, const float *b, const float *c, const f
   if (!pluecker(ld3(a), ld3(b), ld3(c), ld3(o), ld3(d), mode, &h)) return 0;
   tuv[0] = h.t; tuv[1] = h.u; tuv[2] = h.v;
   return 1;
+}
+
+// Normal Ng of PlueckerTriangleIntersect (intersector.hpp:88) for ray i and
+// original triangle prim[i], as the reference writes it to BVHRayHit::hit_ng
+// (radix_bvh.cpp:233); ng[i] = 0 where prim[i] < 0 or the test rejects.
+ORC_API void orc_hit_normals(const float *pos, const int32_t *idx, int64_t n_tri, const float *rays,
+                             int64_t n, const int32_t *prim, int32_t mode, float *ng) {
+  Mesh M{pos, idx, n_tri};
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    V3 N{0.0f, 0.0f, 0.0f};
+    if (prim[i] >= 0) {
+      RayIn r = make_ray(rays, i, n);
+      Hit h;
+      V3 Nh;
+      if (pluecker(ld3(M.v(prim[i], 0)), ld3(M.v(prim[i], 1)), ld3(M.v(prim[i], 2)), ld3(r.o), ld3(r.d), mode,
+                   &h, &Nh))
+        N = Nh;
+    }
+    ng[3 * i] = N.x;
+    ng[3 * i + 1] = N.y;
+    ng[3 * i + 2] = N.z;
+  }
 }
 
 // FP64 t, u, v of ray i against original triangle prim[i] (the FP64 oracle

@@ -42,7 +42,7 @@ def lib() -> C.CDLL:
         _lib.orc_grid_majorant.argtypes = [C.c_void_p, C.c_int64]
         _lib.orc_hg_p.restype = C.c_float
         _lib.orc_num_threads.restype = C.c_int
-        for name in ("orc_stream_uniforms", "orc_volume_tr", "orc_volume_tr64", "orc_volume_tr_adjoint",
+        for name in ("orc_hit_normals", "orc_stream_uniforms", "orc_volume_tr", "orc_volume_tr64", "orc_volume_tr_adjoint",
                      "orc_volume_sample"):
             getattr(_lib, name).restype = None
     return _lib
@@ -219,6 +219,17 @@ def pluecker(a, b, c, o, d, mode=MODE_REF):
     ok = lib().orc_pluecker(_p(_f32(a)), _p(_f32(b)), _p(_f32(c)), _p(_f32(o)), _p(_f32(d)), C.c_int32(mode),
                             _p(out))
     return (bool(ok), out)
+
+
+def hit_normals(pos, idx, n_tri, rays, prim, mode=MODE_DEFECT):
+    """Normal Ng of the Pluecker test of ray i against original triangle
+    prim[i] ([n, 3] float32), as the reference stores it in BVHRayHit::hit_ng."""
+    pos, idx, r = _f32(pos), _i32(idx), _rays8(rays)
+    n = r.shape[1]
+    ng = np.zeros((n, 3), np.float32)
+    lib().orc_hit_normals(_p(pos), _p(idx), C.c_int64(n_tri), _p(r), C.c_int64(n), _p(_i32(prim)),
+                          C.c_int32(mode), _p(ng))
+    return ng
 
 
 def hit_values64(pos, idx, n_tri, rays, prim):
