@@ -67,6 +67,17 @@ class Context:
     def check(self, code: int) -> None:
         check(code, self.h)
 
+    def set_stage_timing(self, on: bool = True) -> None:
+        """Records an event at the end of every build / trace stage."""
+        check(self.lib.flg_ctx_set_stage_timing(self.h, 1 if on else 0), self.h)
+
+    def stage_times(self) -> dict:
+        """{stage: {"ms": summed milliseconds, "n": count}} since the last read."""
+        import json
+        buf = C.create_string_buffer(1 << 16)
+        check(self.lib.flg_ctx_stage_times(self.h, buf, len(buf)), self.h)
+        return json.loads(buf.value.decode() or "{}")
+
     def close(self) -> None:
         if getattr(self, "h", None):
             self.lib.flg_ctx_destroy(self.h)

@@ -91,6 +91,8 @@ SIGNATURES = {
     "flg_ctx_stream": [P],
     "flg_ctx_launch_count": [P],
     "flg_ctx_set_spin_limit": [P, U32],
+    "flg_ctx_set_stage_timing": [P, I32],
+    "flg_ctx_stage_times": [P, C.c_char_p, C.c_size_t],
     "flg_status_string": [C.c_int],
     "flg_debug_wait_unset_flag": [P, U32],
     "flg_ctx_last_error": [P, C.c_char_p, C.c_size_t],

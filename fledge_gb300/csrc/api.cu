@@ -110,7 +110,55 @@ FLG_API int flg_ctx_destroy(flg_ctx c) {
   cudaFree(c->stage);
   cudaFree(c->pt_buf);
   cudaFree(c->rs_buf);
+  for (cudaEvent_t e : c->stage_pool) cudaEventDestroy(e);
   delete c;
+  return FLG_OK;
+}
+
+FLG_API int flg_ctx_set_stage_timing(flg_ctx c, int32_t on) {
+  if (!c) return FLG_ERR_ARG;
+  c->stage_timing = on != 0;
+  c->stage_marks.clear();
+  return FLG_OK;
+}
+
+FLG_API int flg_ctx_stage_times(flg_ctx c, char *json, size_t len) {
+  if (!c || !json || len == 0) return c ? set_error(c, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
+  json[0] = 0;
+  // per stage name (first-seen order): summed milliseconds and count
+  std::vector<const char *> names;
+  std::vector<double> ms;
+  std::vector<int64_t> cnt;
+  if (!c->stage_marks.empty()) {
+    FLG_CUDA(c, cudaEventSynchronize(c->stage_marks.back().second));
+    for (size_t k = 1; k < c->stage_marks.size(); ++k) {
+      const char *nm = c->stage_marks[k].first;
+      if (std::string(nm) == "start") continue;
+      float t = 0.0f;
+      FLG_CUDA(c, cudaEventElapsedTime(&t, c->stage_marks[k - 1].second, c->stage_marks[k].second));
+      size_t j = 0;
+      while (j < names.size() && std::string(names[j]) != nm) ++j;
+      if (j == names.size()) {
+        names.push_back(nm);
+        ms.push_back(0.0);
+        cnt.push_back(0);
+      }
+      ms[j] += t;
+      cnt[j] += 1;
+    }
+  }
+  std::string out = "{";
+  char buf[160];
+  for (size_t j = 0; j < names.size(); ++j) {
+    snprintf(buf, sizeof buf, "%s\"%s\": {\"ms\": %.6f, \"n\": %lld}", j ? ", " : "", names[j], ms[j],
+             (long long)cnt[j]);
+    out += buf;
+  }
+  out += "}";
+  c->stage_marks.clear();
+  if (out.size() + 1 > len) return set_error(c, FLG_ERR_ARG, "stage-time buffer too small (%zu bytes needed)",
+                                             out.size() + 1);
+  memcpy(json, out.c_str(), out.size() + 1);
   return FLG_OK;
 }
 

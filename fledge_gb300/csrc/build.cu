@@ -436,6 +436,7 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
   cudaStream_t st = ctx->stream;
   const int64_t n = b->n_tri;
   if (n <= 0) return FLG_OK;
+  stage_mark(ctx, st, "start");
   const unsigned fill_grid = grid_for(b->n_scenes, 128);
   k_init_boxes<<<fill_grid, 128, 0, st>>>(b->d_scene_box, b->n_scenes);
   FLG_LAUNCH_CHECK(ctx, "k_init_boxes");
@@ -444,6 +445,7 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
     k_scene_bounds<<<grid_for(n, kBoundsChunk), kBoundsThreads, 0, st>>>(b->pos, b->idx, n, b->d_tri_off,
                                                                        b->n_scenes, b->d_scene_box);
     FLG_LAUNCH_CHECK(ctx, "k_scene_bounds");
+    stage_mark(ctx, st, "bounds");
     int rc = sah_build(ctx, b);
     if (rc) return rc;
     if (b->width > 2) return collapse_enqueue(ctx, b, b->width, b->leaf_size);
@@ -462,10 +464,12 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
   FLG_CUDA(ctx, cudaMemsetAsync(b->d_lookback, 0,
                                 sizeof(uint32_t) * 256 * (size_t)b->n_tiles * b->n_passes, st));
   FLG_CUDA(ctx, cudaMemsetAsync(b->d_tile_ctr, 0, sizeof(uint32_t) * b->n_passes, st));
+  stage_mark(ctx, st, "setup");
 
   k_scene_bounds<<<grid_for(n, kBoundsChunk), kBoundsThreads, 0, st>>>(b->pos, b->idx, n, b->d_tri_off,
                                                                      b->n_scenes, b->d_scene_box);
   FLG_LAUNCH_CHECK(ctx, "k_scene_bounds");
+  stage_mark(ctx, st, "bounds");
   uint32_t *morton_out = (b->n_passes % 2 == 0) ? b->d_keys : b->d_keys_alt;
   if (b->d_tile_start) {
     k_morton_seg<<<(unsigned)b->n_tiles, 256, 0, st>>>(b->pos, b->idx, b->d_tri_off, b->n_scenes, b->d_tile_start,
@@ -480,11 +484,13 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
                                           morton_out, b->d_hist, b->n_morton_passes);
     FLG_LAUNCH_CHECK(ctx, "k_morton_hist");
   }
+  stage_mark(ctx, st, "morton");
   int rc = sort_enqueue(ctx, b);
   if (rc) return rc;
   if (b->builder == FLG_BUILDER_PLOC) {
     rc = ploc_build(ctx, b);
     if (rc) return rc;
+    stage_mark(ctx, st, "ploc");
     if (b->width > 2) return collapse_enqueue(ctx, b, b->width, b->leaf_size);
     return FLG_OK;
   }
@@ -500,10 +506,12 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
   FLG_LAUNCH_CHECK(ctx, "k_climb_reset");
   k_climb_clean<<<1, 1, 0, st>>>(b->d_dirty);
   FLG_LAUNCH_CHECK(ctx, "k_climb_clean");
+  stage_mark(ctx, st, "climb_reset");
   k_climb<<<grid_for(n, 256, (int64_t)ctx->num_sms * climb_per_sm), 256, 0, st>>>(
       b->pos, b->idx, n, b->d_tri_off, b->n_scenes, b->d_keys, b->d_perm, b->d_nodes2, b->d_flags, b->d_slots,
       b->d_tris, ctx->spin_limit, ctx->d_err, b->d_dirty);
   FLG_LAUNCH_CHECK(ctx, "k_climb");
+  stage_mark(ctx, st, "climb");
   if (b->width > 2) return collapse_enqueue(ctx, b, b->width, b->leaf_size);
   return FLG_OK;
 }

@@ -367,7 +367,9 @@ int collapse_enqueue(flg_ctx ctx, flg_bvh b, int width, int leaf_size) {
                                 cudaMemcpyDeviceToDevice, st));
   FLG_CUDA(ctx, cudaMemcpyAsync(b->d_queue[0], b->d_queue_init, sizeof(int2) * b->n_wide_roots,
                                 cudaMemcpyDeviceToDevice, st));
-  return width == 4 ? collapse_levels<4>(ctx, b) : collapse_levels<8>(ctx, b);
+  const int rc = width == 4 ? collapse_levels<4>(ctx, b) : collapse_levels<8>(ctx, b);
+  if (rc == FLG_OK) stage_mark(ctx, st, "collapse");
+  return rc;
 }
 
 }  // namespace flg

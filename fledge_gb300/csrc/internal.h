@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/flg.h"
@@ -80,6 +81,11 @@ struct flg_ctx_t {
   void *rs_buf = nullptr;
   size_t rs_bytes = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // Stage timing (flg_ctx_set_stage_timing): an event recorded at the end of
+  // every stage of builds and traces, named by the stage; pooled events.
+  bool stage_timing = false;
+  std::vector<cudaEvent_t> stage_pool;
+  std::vector<std::pair<const char *, cudaEvent_t>> stage_marks;
 };
 
 struct flg_bvh_t {
@@ -188,6 +194,29 @@ int cuda_fail(flg_ctx ctx, cudaError_t e, const char *what);
     cudaError_t e_ = cudaGetLastError();                            \
     if (e_ != cudaSuccess) return ::flg::cuda_fail((ctx), e_, what); \
   } while (0)
+
+// Stage timing: records an event named `stage` on `st` when the context's
+// stage timing is on (never during a capture).  The time between two marks is
+// the named stage's; a mark named "start" opens a new sequence.  At most
+// kMaxStageMarks marks are kept between two reads.
+constexpr size_t kMaxStageMarks = 4096;
+inline void stage_mark(flg_ctx ctx, cudaStream_t st, const char *stage) {
+  if (!ctx->stage_timing || ctx->capturing || ctx->stage_marks.size() >= kMaxStageMarks) return;
+  const size_t k = ctx->stage_marks.size();
+  if (k >= ctx->stage_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    ctx->stage_pool.push_back(e);
+  }
+  if (cudaEventRecord(ctx->stage_pool[k], st) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  ctx->stage_marks.emplace_back(stage, ctx->stage_pool[k]);
+}
 
 // Device allocation owned by a handle.
 template <class T>

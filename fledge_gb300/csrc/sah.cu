@@ -606,6 +606,7 @@ int sah_build(flg_ctx ctx, flg_bvh b) {
     FLG_CUDA(ctx, cudaStreamSynchronize(st));
     cur = nxt;
   }
+  stage_mark(ctx, st, "sah_levels");
   return FLG_OK;
 }
 

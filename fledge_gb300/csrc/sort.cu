@@ -315,6 +315,7 @@ int sort_enqueue(flg_ctx ctx, flg_bvh b) {
                 off + (size_t)p * kRadix, b->d_tile_start, scene_stride, lb, b->d_tile_ctr + p, ctx->d_err,
                 ctx->spin_limit);
     FLG_LAUNCH_CHECK(ctx, "k_onesweep");
+    stage_mark(ctx, ctx->stream, scene_pass ? "sort_scene_pass" : "sort_pass");
   }
   return FLG_OK;
 }
@@ -338,6 +339,7 @@ int sort_pairs_enqueue(flg_ctx ctx, cudaStream_t st, int64_t n, int passes, uint
                 8 * p, nullptr, 1, off + (size_t)p * kRadix, nullptr, 0, lb, tile_ctr + p, ctx->d_err,
                 ctx->spin_limit);
     FLG_LAUNCH_CHECK(ctx, "k_onesweep");
+    stage_mark(ctx, st, "ray_sort_pass");
   }
   return FLG_OK;
 }

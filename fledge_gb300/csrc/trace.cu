@@ -846,6 +846,7 @@ static int finish_enqueue(flg_ctx ctx, cudaStream_t st, const RaySoA &R, int64_t
   if (any || n <= 0) return FLG_OK;
   k_trace_finish<<<grid_for(n, 256, (int64_t)ctx->num_sms * 16), 256, 0, st>>>(R, n, O, b->d_tris);
   FLG_LAUNCH_CHECK(ctx, "k_trace_finish");
+  stage_mark(ctx, st, "trace_finish");
   return FLG_OK;
 }
 
@@ -923,6 +924,7 @@ int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_ra
   Out O{hits ? hits->prim : nullptr, hits ? hits->t : nullptr, hits ? hits->u : nullptr,
         hits ? hits->v : nullptr, occ};
   Scratch S = scratch_for(ctx, set);
+  stage_mark(ctx, st, "start");
   FLG_CUDA(ctx, cudaMemsetAsync(S.ovf_count, 0, sizeof(uint32_t), st));
   FLG_CUDA(ctx, cudaMemsetAsync(S.work, 0, sizeof(unsigned long long), st));
   const bool any = occ != nullptr;
@@ -937,6 +939,7 @@ int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_ra
       k_trace_bvh2<false, true><<<g, 256, 0, st>>>(b->d_nodes2, b->d_tris, b->d_root, ray_off_dev, n_scenes, R, n, O,
                                                    S);
     FLG_LAUNCH_CHECK(ctx, "trace kernel");
+    stage_mark(ctx, st, "trace");
     const unsigned rg = (unsigned)ctx->num_sms;
     if (any)
       k_trace_retry<2, true, true><<<rg, 128, 0, st>>>(nullptr, b->d_nodes2, b->d_tris, b->d_root, ray_off_dev,
@@ -945,6 +948,7 @@ int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_ra
       k_trace_retry<2, false, true><<<rg, 128, 0, st>>>(nullptr, b->d_nodes2, b->d_tris, b->d_root, ray_off_dev,
                                                         n_scenes, R, O, S);
     FLG_LAUNCH_CHECK(ctx, "trace retry kernel");
+    stage_mark(ctx, st, "trace_retry");
     return finish_enqueue(ctx, st, R, n, O, b, any);
   }
   if (b->width == 2) {
@@ -961,6 +965,7 @@ int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_ra
     else launch_wide<8, false>(ctx, st, b, R, n, O, S, ray_off_dev, n_scenes, op);
   }
   FLG_LAUNCH_CHECK(ctx, "trace kernel");
+  stage_mark(ctx, st, "trace");
   const unsigned rg = (unsigned)ctx->num_sms;
   const void *wide = b->d_wide;
   const int32_t *roots = b->width == 2 ? b->d_root : b->d_wide_root;
@@ -980,6 +985,7 @@ int trace_enqueue(flg_ctx ctx, cudaStream_t st, int set, flg_bvh b, const flg_ra
   }
 #undef FLG_RETRY
   FLG_LAUNCH_CHECK(ctx, "trace retry kernel");
+  stage_mark(ctx, st, "trace_retry");
   return finish_enqueue(ctx, st, R, n, O, b, any);
 }
 

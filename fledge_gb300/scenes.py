@@ -1,14 +1,28 @@
-"""Seeded synthetic scenes for the path-tracing workload (host-side input
-generation, numpy).
+"""Seeded synthetic workloads (host-side input generation).
 
 * ``icosphere``: an icosahedron subdivided `level` times (20 * 4^level
   triangles) on a sphere of radius `radius`, each vertex displaced radially
   by ``amplitude * noise(p)`` with 4-octave value noise.
 * ``quad_light``: the 0.2 x 0.2 emitter at y = 2 facing -y, as 2 triangles.
+* ``path_tracing_scene`` / ``PATH_TRACING_CAMERA``: the level-8 icosphere
+  (1,310,720 triangles) under the light, and its 1920x1080 camera.
+* ``batched_scene_counts``: triangle counts of the 256-scene batch,
+  round(exp(U[ln 1e3, ln 1e6])).
+* ``camera_rays_4k``: the 3840x2160x4 jittered pinhole rays of the
+  8 M-triangle scene (device tensors).
+
+Seeds are 0xF1ED0000 + k for workload k (0: random soup, 1: path tracing,
+2: volume, 3: batched scenes).
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
+
+SEED_SOUP, SEED_PATH, SEED_VOLUME, SEED_BATCH = 0xF1ED0000, 0xF1ED0001, 0xF1ED0002, 0xF1ED0003
+N_SCENES = 256
+RAYS_PER_TRI = 64
 
 _PHI = (1.0 + 5.0 ** 0.5) / 2.0
 _ICO_V = np.array([[-1, _PHI, 0], [1, _PHI, 0], [-1, -_PHI, 0], [1, -_PHI, 0],
@@ -87,3 +101,42 @@ def quad_light(y: float = 2.0, half: float = 0.1):
     # winding so that (p1-p0) x (p2-p0) points down (-y)
     f = np.array([[0, 1, 2], [0, 2, 3]], np.int32)
     return v, f
+
+
+def path_tracing_scene(level: int = 8):
+    """(positions, indices, first light triangle): the displaced icosphere
+    followed by the two light triangles."""
+    v, f = icosphere(level)
+    lv, lf = quad_light()
+    return np.concatenate([v, lv], 0), np.concatenate([f, lf + len(v)], 0), len(f)
+
+
+PATH_TRACING_CAMERA = dict(eye=(0.0, 0.6, 3.5), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), fov_deg=40.0)
+
+
+def batched_scene_counts(n_scenes: int = N_SCENES, seed: int = SEED_BATCH) -> np.ndarray:
+    """Triangle counts of the batched workload, log-uniform in [1e3, 1e6]."""
+    rng = np.random.default_rng(seed)
+    c = np.round(np.exp(rng.uniform(math.log(1e3), math.log(1e6), N_SCENES))).astype(np.int64)
+    return c[:n_scenes]
+
+
+def camera_rays_4k(torch, device, seed: int = SEED_BATCH + 41, width: int = 3840, height: int = 2160,
+                   spp: int = 4):
+    """Jittered pinhole camera rays (6 x n device tensor, SoA ox..dz) from
+    (0.5, 0.5, -1.5) looking along +z with a 45 degree vertical field of
+    view, spp samples per pixel in pixel-major order."""
+    n = width * height * spp
+    g = torch.Generator(device=device).manual_seed(seed)
+    pix = torch.arange(n, device=device)
+    px = (pix // spp) % width
+    py = (pix // spp) // width
+    jx = torch.rand(n, device=device, generator=g)
+    jy = torch.rand(n, device=device, generator=g)
+    tan = math.tan(math.radians(22.5))
+    sx = ((px.float() + jx) / width * 2 - 1) * tan * (width / height)
+    sy = (1 - (py.float() + jy) / height * 2) * tan
+    d = torch.stack([sx, sy, torch.ones_like(sx)], 0)
+    d = d / d.norm(dim=0, keepdim=True)
+    o = torch.tensor([0.5, 0.5, -1.5], device=device)[:, None].expand(3, n)
+    return torch.cat([o, d], 0).contiguous()

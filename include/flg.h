@@ -127,6 +127,18 @@ FLG_API int64_t flg_ctx_launch_count(flg_ctx ctx);
 /* Test hook: caps every bounded device-side spin-wait at `spins` iterations
  * (0 restores the default).  Used to inject FLG_ERR_TIMEOUT from the host. */
 FLG_API int flg_ctx_set_spin_limit(flg_ctx ctx, uint32_t spins);
+/* Stage timing (no counterpart in the reference, which prints whole-build
+ * timings only, bvh_test.hpp:30-36): with `on`, every build and trace issued
+ * on ctx records a CUDA event at the end of each of its stages (setup,
+ * bounds, morton, sort, climb, collapse, trace, trace_retry, trace_finish,
+ * and the SAH / PLOC stages); nothing is recorded during a stream capture.
+ * Turning it on or off discards the recorded marks. */
+FLG_API int flg_ctx_set_stage_timing(flg_ctx ctx, int32_t on);
+/* Waits for the last mark and writes the recorded stage times as a JSON
+ * object {"stage": {"ms": summed milliseconds, "n": occurrences}, ...} in
+ * first-seen order, then discards the marks.  FLG_ERR_ARG if json_len is too
+ * small. */
+FLG_API int flg_ctx_stage_times(flg_ctx ctx, char *json, size_t json_len);
 FLG_API const char *flg_status_string(int status);
 /* Test hook: launches one thread that waits, with the library's bounded
  * spin-wait, on a device word that nothing ever sets, then synchronises.

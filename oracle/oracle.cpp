@@ -543,9 +543,11 @@ struct Grid {
     float c1 = lerp(c01, c11, fy);
     return lerp(c0, c1, fz);
   }
-  inline double at64(int x, int y, int z, const double *r64) const {
+  inline double at64(int x, int y, int z, const double *r64, int64_t pv = -1, double pd = 0.0) const {
     if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) return 0.0;
-    return r64 ? r64[((int64_t)z * ny + y) * nx + x] : (double)rho[((int64_t)z * ny + y) * nx + x];
+    const int64_t v = ((int64_t)z * ny + y) * nx + x;
+    const double r = r64 ? r64[v] : (double)rho[v];
+    return v == pv ? r + pd : r;
   }
 };
 
@@ -605,7 +607,7 @@ float ratio_track(const Grid &G, const float *o, const float *d, float tmax, Ray
 // Same estimator in double precision (the FP64 oracle); the random draws are
 // the same uniforms.  rho64 (optional) overrides the grid values.
 double ratio_track64(const Grid &G, const double *rho64, const float *o, const float *d, float tmax,
-                     RayStream &rs, int *n_rr) {
+                     RayStream &rs, int *n_rr, int64_t pv = -1, double pd = 0.0) {
   double t0 = 0.0, t1 = tmax;
   for (int i = 0; i < 3; ++i) {
     double inv = 1.0 / (double)d[i];
@@ -633,7 +635,7 @@ double ratio_track64(const Grid &G, const double *rho64, const float *o, const f
     for (int c = 0; c < 8; ++c) {
       int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
       double w = (cx ? fx : 1.0 - fx) * (cy ? fy : 1.0 - fy) * (cz ? fz : 1.0 - fz);
-      den += w * G.at64(x + cx, y + cy, z + cz, rho64);
+      den += w * G.at64(x + cx, y + cy, z + cz, rho64, pv, pd);
     }
     tr *= 1.0 - std::max(0.0, den * inv_maxd);
     if (tr < (double)G.rr) {
@@ -1185,12 +1187,73 @@ ORC_API void orc_volume_tr64(const float *rho, const double *rho64, int nx, int 
   }
 }
 
+// FP64 ratio tracking of a subset of rays: ray j of the arrays is ray
+// ray_ids[j] of the full set (its Philox stream), and grid value `vox` (-1:
+// none) is raised by `delta` in double precision.  For central finite
+// differences on large grids without copying them.
+ORC_API void orc_volume_tr64_sub(const float *rho, int nx, int ny, int nz, const float *lo, const float *hi,
+                                 const OrcMedium *m, const float *rays, int64_t n, const int64_t *ray_ids,
+                                 uint64_t seed, int64_t vox, double delta, double *T, int32_t *n_rr) {
+  Grid G = make_grid(rho, nx, ny, nz, lo, hi, m);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < n; ++i) {
+    float o[3] = {rays[i], rays[n + i], rays[2 * n + i]};
+    float d[3] = {rays[3 * n + i], rays[4 * n + i], rays[5 * n + i]};
+    RayStream rs = stream_for(seed, ray_ids[i]);
+    int nr = 0;
+    T[i] = ratio_track64(G, nullptr, o, d, rays[7 * n + i], rs, &nr, vox, delta);
+    if (n_rr) n_rr[i] = nr;
+  }
+}
+
 // Adjoint of ratio tracking with respect to the grid, fp32 forward arithmetic
 // (identical to the GPU's) and FP64 accumulation:
 //   T = c * prod_{i in last segment} (1 - d_i / rho_max),
 //   dT/drho_v = sum_i -T / (1 - d_i/rho_max) * w_iv / rho_max,
 // with the majorant held constant (steps do not move with the grid) and the
 // roulette rescale 1/(1-q) = 1/T contributing nothing (T is reset to ~1).
+namespace {
+// One ray's adjoint: replays its stream from the last roulette checkpoint and
+// calls emit(flat voxel index, dL/drho contribution) for every lattice point
+// of every step after it.
+template <typename Emit>
+void tr_adjoint_ray(const Grid &G, const float *o, const float *d, float tmax, uint64_t seed, int64_t ray,
+                    float dL, Emit &&emit) {
+  RayStream rs = stream_for(seed, ray);
+  TrState ck;
+  float Tf = ratio_track(G, o, d, tmax, rs, &ck);
+  if (Tf == 0.0f || dL == 0.0f) return;
+  float t_min, t_max;
+  if (!box_intersect_pbrt(G, o, d, tmax, &t_min, &t_max)) return;
+  t_max = std::min(t_max, tmax);
+  float max_mu = G.sigma_t * G.maxd;
+  RayStream r2 = stream_for(seed, ray);
+  r2.k = ck.k;
+  float t = ck.t;
+  for (int step_ = 0; step_ < kMaxTrackSteps; ++step_) {
+    float u = r2.next();
+    t += -flg_logf(1.0f - u) / max_mu;
+    if (t >= t_max) break;
+    float pos[3] = {o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t};
+    int b[3];
+    float f[3];
+    float den = G.sample(pos, b, f);
+    float x = den * G.inv_maxd;
+    if (!(x > 0.0f)) continue;
+    double fac = 1.0 - (double)x;
+    double coef = -(double)dL * (double)Tf * (double)G.inv_maxd / fac;
+    for (int c = 0; c < 8; ++c) {
+      int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
+      int X = b[0] + cx, Y = b[1] + cy, Z = b[2] + cz;
+      if (X < 0 || Y < 0 || Z < 0 || X >= G.nx || Y >= G.ny || Z >= G.nz) continue;
+      double w = (cx ? (double)f[0] : 1.0 - f[0]) * (cy ? (double)f[1] : 1.0 - f[1]) *
+                 (cz ? (double)f[2] : 1.0 - f[2]);
+      emit(((int64_t)Z * G.ny + Y) * G.nx + X, coef * w);
+    }
+  }
+}
+}  // namespace
+
 ORC_API void orc_volume_tr_adjoint(const float *rho, int nx, int ny, int nz, const float *lo,
                                    const float *hi, const OrcMedium *m, const float *rays, int64_t n,
                                    uint64_t seed, const float *dLdT, double *grad) {
@@ -1198,39 +1261,26 @@ ORC_API void orc_volume_tr_adjoint(const float *rho, int nx, int ny, int nz, con
   for (int64_t i = 0; i < n; ++i) {
     float o[3] = {rays[i], rays[n + i], rays[2 * n + i]};
     float d[3] = {rays[3 * n + i], rays[4 * n + i], rays[5 * n + i]};
-    float tmax = rays[7 * n + i];
-    RayStream rs = stream_for(seed, i);
-    TrState ck;
-    float Tf = ratio_track(G, o, d, tmax, rs, &ck);
-    if (Tf == 0.0f || dLdT[i] == 0.0f) continue;
-    float t_min, t_max;
-    if (!box_intersect_pbrt(G, o, d, tmax, &t_min, &t_max)) continue;
-    t_max = std::min(t_max, tmax);
-    float max_mu = G.sigma_t * G.maxd;
-    RayStream r2 = stream_for(seed, i);
-    r2.k = ck.k;
-    float t = ck.t;
-    for (int step_ = 0; step_ < kMaxTrackSteps; ++step_) {
-      float u = r2.next();
-      t += -flg_logf(1.0f - u) / max_mu;
-      if (t >= t_max) break;
-      float pos[3] = {o[0] + d[0] * t, o[1] + d[1] * t, o[2] + d[2] * t};
-      int b[3];
-      float f[3];
-      float den = G.sample(pos, b, f);
-      float x = den * G.inv_maxd;
-      if (!(x > 0.0f)) continue;
-      double fac = 1.0 - (double)x;
-      double coef = -(double)dLdT[i] * (double)Tf * (double)G.inv_maxd / fac;
-      for (int c = 0; c < 8; ++c) {
-        int cx = c & 1, cy = (c >> 1) & 1, cz = c >> 2;
-        int X = b[0] + cx, Y = b[1] + cy, Z = b[2] + cz;
-        if (X < 0 || Y < 0 || Z < 0 || X >= nx || Y >= ny || Z >= nz) continue;
-        double w = (cx ? (double)f[0] : 1.0 - f[0]) * (cy ? (double)f[1] : 1.0 - f[1]) *
-                   (cz ? (double)f[2] : 1.0 - f[2]);
-        grad[((int64_t)Z * ny + Y) * nx + X] += coef * w;
-      }
-    }
+    tr_adjoint_ray(G, o, d, rays[7 * n + i], seed, i, dLdT[i], [&](int64_t v, double g) { grad[v] += g; });
+  }
+}
+
+// Per-ray contributions to dT/drho at one voxel (flat index vox), dL/dT = 1,
+// for a subset of rays: ray j of the arrays is ray ray_ids[j] of the full set
+// (its Philox stream).  out: n doubles.
+ORC_API void orc_volume_tr_adjoint_vox(const float *rho, int nx, int ny, int nz, const float *lo,
+                                       const float *hi, const OrcMedium *m, const float *rays, int64_t n,
+                                       const int64_t *ray_ids, uint64_t seed, int64_t vox, double *out) {
+  Grid G = make_grid(rho, nx, ny, nz, lo, hi, m);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t i = 0; i < n; ++i) {
+    float o[3] = {rays[i], rays[n + i], rays[2 * n + i]};
+    float d[3] = {rays[3 * n + i], rays[4 * n + i], rays[5 * n + i]};
+    double acc = 0.0;
+    tr_adjoint_ray(G, o, d, rays[7 * n + i], seed, ray_ids[i], 1.0f, [&](int64_t v, double g) {
+      if (v == vox) acc += g;
+    });
+    out[i] = acc;
   }
 }
 

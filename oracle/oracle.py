@@ -42,7 +42,7 @@ def lib() -> C.CDLL:
         _lib.orc_grid_majorant.argtypes = [C.c_void_p, C.c_int64]
         _lib.orc_hg_p.restype = C.c_float
         _lib.orc_num_threads.restype = C.c_int
-        for name in ("orc_hit_normals", "orc_stream_uniforms", "orc_volume_tr", "orc_volume_tr64", "orc_volume_tr_adjoint",
+        for name in ("orc_hit_normals", "orc_volume_tr64_sub", "orc_volume_tr_adjoint_vox", "orc_stream_uniforms", "orc_volume_tr", "orc_volume_tr64", "orc_volume_tr_adjoint",
                      "orc_volume_sample"):
             getattr(_lib, name).restype = None
     return _lib
@@ -283,6 +283,23 @@ def volume_tr64(rho, lo, hi, medium, rays, seed, rho64=None):
     return T, nrr
 
 
+def volume_tr64_sub(rho, lo, hi, medium, rays, ray_ids, seed, vox=-1, delta=0.0):
+    """FP64 ratio tracking of a subset of rays (ray j draws from the stream of
+    ray ray_ids[j]) with grid value `vox` (flat index) raised by `delta`.
+    Returns (T, roulette counts)."""
+    rho = _f32(rho)
+    nz, ny, nx = rho.shape
+    r = _rays8(rays)
+    n = r.shape[1]
+    ids = np.ascontiguousarray(ray_ids, np.int64)
+    T = np.zeros(n, np.float64)
+    nrr = np.zeros(n, np.int32)
+    m = _medium(medium)
+    lib().orc_volume_tr64_sub(_p(rho), nx, ny, nz, _p(_f32(lo)), _p(_f32(hi)), C.byref(m), _p(r), C.c_int64(n),
+                              _p(ids), C.c_uint64(seed), C.c_int64(vox), C.c_double(delta), _p(T), _p(nrr))
+    return T, nrr
+
+
 def volume_tr_adjoint(rho, lo, hi, medium, rays, seed, dLdT):
     rho = _f32(rho)
     nz, ny, nx = rho.shape
@@ -293,6 +310,21 @@ def volume_tr_adjoint(rho, lo, hi, medium, rays, seed, dLdT):
     lib().orc_volume_tr_adjoint(_p(rho), nx, ny, nz, _p(_f32(lo)), _p(_f32(hi)), C.byref(m), _p(r), C.c_int64(n),
                                 C.c_uint64(seed), _p(_f32(dLdT)), _p(grad))
     return grad
+
+
+def volume_tr_adjoint_vox(rho, lo, hi, medium, rays, ray_ids, seed, vox):
+    """Per-ray contributions (dL/dT = 1) to the gradient at one voxel (flat
+    index) for a subset of rays keyed by ray_ids."""
+    rho = _f32(rho)
+    nz, ny, nx = rho.shape
+    r = _rays8(rays)
+    n = r.shape[1]
+    ids = np.ascontiguousarray(ray_ids, np.int64)
+    out = np.zeros(n, np.float64)
+    m = _medium(medium)
+    lib().orc_volume_tr_adjoint_vox(_p(rho), nx, ny, nz, _p(_f32(lo)), _p(_f32(hi)), C.byref(m), _p(r),
+                                    C.c_int64(n), _p(ids), C.c_uint64(seed), C.c_int64(vox), _p(out))
+    return out
 
 
 def volume_sample(rho, lo, hi, medium, rays, seed):
