@@ -211,6 +211,18 @@ class RadixBVHBuilder:
                                                       C.byref(hs)))
         return out
 
+    def hit_normals(self, rays: Rays, prim, kind: str = "pluecker", out=None):
+        """Normals of fixed hits, [n, 3]: "pluecker" (BVHRayHit::hit_ng of the
+        experimental path) or "geometric" (SInteraction::m_ng of the live
+        renderer's triangle test)."""
+        torch = _torch()
+        k = {"pluecker": 0, "geometric": 1}[kind]
+        out = out if out is not None else torch.empty((rays.n, 3), dtype=torch.float32, device=prim.device)
+        r = rays.struct()
+        self.ctx.check(self.ctx.lib.flg_hit_normals(self.ctx.h, self.h, C.byref(r), rays.n, C.c_void_p(_ptr(prim)),
+                                                    k, C.c_void_p(_ptr(out))))
+        return out
+
     def intersectP(self, rays: Rays, out=None, **opts):
         """Any hit (occlusion) for a batch of rays: uint8 tensor."""
         torch = _torch()

@@ -110,8 +110,11 @@ SIGNATURES = {
     "flg_trace_closest_noalloc": [P, P, C.POINTER(FlgRays), I64, C.POINTER(FlgHits)],
     "flg_autotune_trace": [P, P, C.POINTER(FlgRays), I64, C.POINTER(FlgTraceOpts), C.POINTER(I32),
                            C.c_char_p, C.c_size_t],
+    "flg_autotune_trace_batched": [P, P, C.POINTER(FlgRays), C.POINTER(I64), I32, C.POINTER(FlgTraceOpts),
+                                   C.POINTER(I32), C.POINTER(I32), C.c_char_p, C.c_size_t],
     "flg_bvh_set_width": [P, P, I32, I32],
     "flg_hit_adjoint": [P, P, P, I64, I64, C.POINTER(FlgRays), I64, C.POINTER(FlgHits), P, P, P, P],
+    "flg_hit_normals": [P, P, C.POINTER(FlgRays), I64, P, I32, P],
     "flg_grid_create": [P, P, I32, I32, I32, C.POINTER(F32), C.POINTER(F32), C.POINTER(FlgMedium), PP],
     "flg_grid_destroy": [P],
     "flg_grid_majorant": [P, C.POINTER(F32)],

@@ -84,3 +84,63 @@ FLG_API int flg_hit_adjoint(flg_ctx ctx, const float *pos, const int32_t *idx, i
   FLG_LAUNCH_CHECK(ctx, "k_hit_adjoint");
   return FLG_OK;
 }
+
+namespace flg {
+
+// Normal of a fixed hit.  kind 0: the Pluecker test's Ng (intersector.hpp:
+// 86-88), StableTriangleNormal of the ray-relative edges in fp32 and the
+// Euclidean normalisation in double; kind 1: the live renderer's
+// normalize(cross(p1 - p0, p2 - p0)) in fp32 (shape.cpp:141, vector.h:
+// 364-404).  Same operation order as those functions; zeros on a miss.
+__global__ void __launch_bounds__(256)
+    k_hit_normals(const float *__restrict__ pos, const int32_t *__restrict__ idx, int64_t n_tri,
+                  const float *__restrict__ ox, const float *__restrict__ oy, const float *__restrict__ oz,
+                  int64_t n, const int32_t *__restrict__ prim, int kind, float *__restrict__ ng) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t p = prim[i];
+  float3 N = make_float3(0.0f, 0.0f, 0.0f);
+  if (p >= 0 && p < n_tri) {
+    float3 a, b, c;
+    tri_verts(pos, idx, p, a, b, c);
+    if (kind == 0) {
+      const float3 O = make_float3(ox[i], oy[i], oz[i]);
+      const float3 v0 = f3sub(a, O), v1 = f3sub(b, O), v2 = f3sub(c, O);
+      const float3 e0 = f3sub(v2, v0), e1 = f3sub(v0, v1), e2 = f3sub(v1, v2);
+      const float ab_x = e0.z * e1.y, ab_y = e0.x * e1.z, ab_z = e0.y * e1.x;
+      const float bc_x = e1.z * e2.y, bc_y = e1.x * e2.z, bc_z = e1.y * e2.x;
+      float3 S;
+      S.x = fabsf(ab_x) < fabsf(bc_x) ? e0.y * e1.z - ab_x : e1.y * e2.z - bc_x;
+      S.y = fabsf(ab_y) < fabsf(bc_y) ? e0.z * e1.x - ab_y : e1.z * e2.x - bc_y;
+      S.z = fabsf(ab_z) < fabsf(bc_z) ? e0.x * e1.y - ab_z : e1.x * e2.y - bc_z;
+      const double x = S.x, y = S.y, z = S.z;
+      const double r = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z)));
+      N = make_float3((float)__ddiv_rn(x, r), (float)__ddiv_rn(y, r), (float)__ddiv_rn(z, r));
+    } else {
+      const float3 C = f3cross(f3sub(b, a), f3sub(c, a));
+      const float s = __fsqrt_rn(f3dot(C, C));
+      N = make_float3(__fdiv_rn(C.x, s), __fdiv_rn(C.y, s), __fdiv_rn(C.z, s));
+    }
+  }
+  ng[3 * i] = N.x;
+  ng[3 * i + 1] = N.y;
+  ng[3 * i + 2] = N.z;
+}
+
+}  // namespace flg
+
+FLG_API int flg_hit_normals(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n, const int32_t *prim,
+                            int32_t kind, float *ng) {
+  if (!ctx) return FLG_ERR_ARG;
+  if (!bvh || !rays || !prim || !ng || n < 0) return set_error(ctx, FLG_ERR_ARG, "NULL argument or negative n");
+  if (kind != FLG_NORMAL_PLUECKER && kind != FLG_NORMAL_GEOMETRIC)
+    return set_error(ctx, FLG_ERR_ARG, "kind must be FLG_NORMAL_PLUECKER or FLG_NORMAL_GEOMETRIC");
+  if (bvh->n_scenes != 1) return set_error(ctx, FLG_ERR_ARG, "batched handle: normals take one scene");
+  if (kind == FLG_NORMAL_PLUECKER && (!rays->ox || !rays->oy || !rays->oz))
+    return set_error(ctx, FLG_ERR_ARG, "ray origins are NULL");
+  if (n == 0) return FLG_OK;
+  k_hit_normals<<<(unsigned)ceil_div(n, 256), 256, 0, ctx->stream>>>(bvh->pos, bvh->idx, bvh->n_tri, rays->ox,
+                                                                      rays->oy, rays->oz, n, prim, kind, ng);
+  FLG_LAUNCH_CHECK(ctx, "k_hit_normals");
+  return FLG_OK;
+}

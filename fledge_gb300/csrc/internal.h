@@ -71,6 +71,7 @@ struct flg_ctx_t {
   unsigned long long *d_work = nullptr;  // [0] persistent ray counter
   int64_t *d_ray_off = nullptr;          // device copy of batched ray offsets
   int64_t ray_off_cap = 0;
+  std::vector<int64_t> ray_off_h;        // host copy of what d_ray_off holds
   // Device staging buffers for flg_trace_closest_host (grown on demand).
   void *stage = nullptr;
   size_t stage_bytes = 0;

@@ -1031,7 +1031,7 @@ FLG_API int flg_trace_closest_batched(flg_ctx ctx, flg_bvh bvh, const flg_rays *
     return set_error(ctx, FLG_ERR_ARG, "hit output pointer is NULL");
   // Device copy of the offsets, refreshed only when they change (so a
   // captured graph replays without a host copy).
-  static thread_local std::vector<int64_t> cached;
+  std::vector<int64_t> &cached = ctx->ray_off_h;
   bool same = ctx->d_ray_off && ctx->ray_off_cap >= ns + 1 && cached.size() == (size_t)(ns + 1) &&
               std::equal(cached.begin(), cached.end(), ray_offsets_host);
   if (!same) {
@@ -1103,124 +1103,194 @@ FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *rh,
   return flg_ctx_sync(ctx);
 }
 
+namespace flg {
+
+// Staged search of the traversal configuration on a given workload (node
+// width and leaf size, then the kernel, then the block size; single-scene
+// handles also try the ray-sort key).  Every trial is one untimed launch and
+// `reps` launches timed one by one with events; the trial's time is their
+// median.  Leaves the handle at the fastest layout.
+struct Tuner {
+  flg_ctx ctx;
+  flg_bvh bvh;
+  const flg_rays *rays;
+  int64_t n;
+  const int64_t *ray_off;
+  int n_scenes, reps;
+  flg_hits h;
+  std::vector<cudaEvent_t> ev;
+  std::string rec = "{\"trials\": [";
+  bool first = true;
+  float best_ms = 1e30f;
+  flg_trace_opts best{};
+  int best_w = 4, best_leaf = 1;
+
+  int trial(int w, int leaf, const flg_trace_opts &op, const char *stage) {
+    int rc = trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, &op, ray_off, n_scenes, &h, nullptr);
+    if (rc) return rc;
+    for (int r = 0; r < reps; ++r) {
+      FLG_CUDA(ctx, cudaEventRecord(ev[2 * r], ctx->stream));
+      rc = trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, &op, ray_off, n_scenes, &h, nullptr);
+      if (rc) return rc;
+      FLG_CUDA(ctx, cudaEventRecord(ev[2 * r + 1], ctx->stream));
+    }
+    FLG_CUDA(ctx, cudaEventSynchronize(ev[2 * reps - 1]));
+    std::vector<float> ms(reps);
+    for (int r = 0; r < reps; ++r) FLG_CUDA(ctx, cudaEventElapsedTime(&ms[r], ev[2 * r], ev[2 * r + 1]));
+    std::sort(ms.begin(), ms.end());
+    const float med = reps % 2 ? ms[reps / 2] : 0.5f * (ms[reps / 2 - 1] + ms[reps / 2]);
+    char line[384];
+    snprintf(line, sizeof(line),
+             "%s{\"stage\": \"%s\", \"node_width\": %d, \"leaf_size\": %d, \"stack_depth\": %d, \"persistent\": %d, "
+             "\"refill_lanes\": %d, \"block_threads\": %d, \"ray_sort\": %d, \"ms\": %.5f, \"ms_min\": %.5f, "
+             "\"ms_max\": %.5f, \"mrays_s\": %.2f}",
+             first ? "" : ", ", stage, w, leaf, op.stack_depth, op.persistent, op.refill_lanes, op.block_threads,
+             op.ray_sort, med, ms.front(), ms.back(), n / (med * 1e3));
+    first = false;
+    rec += line;
+    if (med < best_ms) {
+      best_ms = med;
+      best = op;
+      best_w = w;
+      best_leaf = leaf;
+    }
+    return FLG_OK;
+  }
+
+  static flg_trace_opts kernel_opts(int w, int pers, int refill, int stack, int threads) {
+    flg_trace_opts op{};
+    op.stack_depth = stack;
+    op.persistent = w == 2 ? 0 : pers;
+    op.refill_lanes = refill;
+    op.block_threads = threads;
+    return op;
+  }
+
+  int run() {
+    int rc;
+    // 1. layout, with the default kernel of each width
+    for (int w : {2, 4, 8}) {
+      for (int leaf : {1, 2, 3, 4}) {
+        if (w == 2 && leaf > 1) continue;
+        rc = flg_bvh_set_width(ctx, bvh, w, leaf);
+        if (rc) return rc;
+        rc = trial(w, leaf, kernel_opts(w, 2, 8, 64, 256), "layout");
+        if (rc) return rc;
+      }
+    }
+    const int w = best_w, leaf = best_leaf;
+    rc = flg_bvh_set_width(ctx, bvh, w, leaf);
+    if (rc) return rc;
+    // 2. kernel on that layout
+    if (w > 2) {
+      for (int pers : {0, 1, 2})
+        for (int refill : {4, 8, 16})
+          for (int stack : {32, 64}) {
+            if (pers == 0 && refill != 8) continue;
+            if (pers == 2 && refill == 8 && stack == 64) continue;  // tried in stage 1
+            rc = trial(w, leaf, kernel_opts(w, pers, refill, stack, 256), "kernel");
+            if (rc) return rc;
+          }
+    } else {
+      rc = trial(w, leaf, kernel_opts(w, 0, 8, 32, 256), "kernel");
+      if (rc) return rc;
+    }
+    // 3. block size
+    {
+      flg_trace_opts op = best;
+      op.block_threads = 128;
+      rc = trial(w, leaf, op, "block");
+      if (rc) return rc;
+    }
+    // 4. ray-sort key (single-scene traces): pays when neighbouring rays are
+    // scattered, costs a sort and two gathers when they are not
+    if (!ray_off && n_scenes == 1 && n <= ((int64_t)1 << 28)) {
+      flg_trace_opts op = best;
+      op.ray_sort = 1;
+      rc = trial(w, leaf, op, "ray_sort");
+      if (rc) return rc;
+    }
+    char tail[384];
+    snprintf(tail, sizeof(tail),
+             "], \"reps\": %d, \"rays\": %lld, \"scenes\": %d, \"best\": {\"node_width\": %d, \"leaf_size\": %d, "
+             "\"stack_depth\": %d, \"persistent\": %d, \"refill_lanes\": %d, \"block_threads\": %d, \"ray_sort\": %d, "
+             "\"ms\": %.5f, \"mrays_s\": %.2f}}",
+             reps, (long long)n, n_scenes, best_w, best_leaf, best.stack_depth, best.persistent, best.refill_lanes,
+             best.block_threads, best.ray_sort, best_ms, n / (best_ms * 1e3));
+    rec += tail;
+    return FLG_OK;
+  }
+};
+
+static int autotune(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n, const int64_t *ray_off,
+                    int n_scenes, int reps, flg_trace_opts *best, int32_t *best_width, int32_t *best_leaf,
+                    char *json, size_t json_len) {
+  if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "autotuning cannot be captured");
+  if (reps < 1 || reps > 64) return set_error(ctx, FLG_ERR_ARG, "reps must be in [1, 64]");
+  if (n <= 0) return set_error(ctx, FLG_ERR_ARG, "autotuning needs rays");
+  void *buf = nullptr;
+  FLG_CUDA(ctx, cudaMalloc(&buf, sizeof(float) * 4 * (size_t)n));
+  Tuner T{ctx, bvh, rays, n, ray_off, n_scenes, reps,
+          flg_hits{(int32_t *)buf, (float *)buf + n, (float *)buf + 2 * n, (float *)buf + 3 * n}};
+  T.ev.assign(2 * reps, nullptr);
+  int rc = FLG_OK;
+  for (auto &e : T.ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      rc = set_error(ctx, FLG_ERR_CUDA, "cudaEventCreate failed");
+      break;
+    }
+  if (!rc) rc = T.run();
+  for (auto &e : T.ev)
+    if (e) cudaEventDestroy(e);
+  cudaFree(buf);
+  if (rc) return rc;
+  *best = T.best;
+  if (best_width) *best_width = T.best_w;
+  if (best_leaf) *best_leaf = T.best_leaf;
+  if (json && json_len) {
+    if (T.rec.size() + 1 > json_len)
+      return set_error(ctx, FLG_ERR_ARG, "json buffer too small (%zu bytes needed)", T.rec.size() + 1);
+    std::memcpy(json, T.rec.c_str(), T.rec.size() + 1);
+  }
+  return flg_ctx_sync(ctx);
+}
+
+}  // namespace flg
+
 FLG_API int flg_autotune_trace(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n, flg_trace_opts *best,
                                int32_t *best_width, char *json, size_t json_len) {
-  if (!ctx || !bvh || !best) return FLG_ERR_ARG;
+  if (!ctx || !bvh || !best) return ctx ? set_error(ctx, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
+  int rc = check_rays(ctx, rays, n);
+  if (rc) return rc;
+  if (bvh->n_scenes != 1) return set_error(ctx, FLG_ERR_ARG, "batched handle: use flg_autotune_trace_batched");
+  return autotune(ctx, bvh, rays, n, nullptr, 1, 5, best, best_width, nullptr, json, json_len);
+}
+
+FLG_API int flg_autotune_trace_batched(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays,
+                                       const int64_t *ray_offsets_host, int32_t reps, flg_trace_opts *best,
+                                       int32_t *best_width, int32_t *best_leaf, char *json, size_t json_len) {
+  if (!ctx || !bvh || !best || !ray_offsets_host)
+    return ctx ? set_error(ctx, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
+  const int ns = bvh->n_scenes;
+  if (ray_offsets_host[0] != 0) return set_error(ctx, FLG_ERR_ARG, "ray_offsets[0] must be 0");
+  for (int s = 0; s < ns; ++s)
+    if (ray_offsets_host[s + 1] < ray_offsets_host[s])
+      return set_error(ctx, FLG_ERR_ARG, "ray_offsets must be non-decreasing");
+  const int64_t n = ray_offsets_host[ns];
   int rc = check_rays(ctx, rays, n);
   if (rc) return rc;
   if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "autotuning cannot be captured");
-  if (bvh->n_scenes != 1) return set_error(ctx, FLG_ERR_ARG, "autotune a single-scene handle");
-  // Scratch outputs.
-  void *buf = nullptr;
-  FLG_CUDA(ctx, cudaMalloc(&buf, sizeof(float) * 4 * (size_t)std::max<int64_t>(n, 1)));
-  flg_hits h{(int32_t *)buf, (float *)buf + n, (float *)buf + 2 * n, (float *)buf + 3 * n};
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  std::string rec = "{\"trials\": [";
-  float best_ms = 1e30f;
-  flg_trace_opts bo{};
-  int bw = bvh->width, bl = bvh->leaf_size;
-  const int orig_w = bvh->width, orig_leaf = bvh->leaf_size;
-  bool first = true;
-  for (int w : {2, 4, 8}) {
-    static const int kLeaves[4] = {1, 2, 3, 4};
-    for (int li = 0; li < (w == 2 ? 1 : 4); ++li) {
-      const int leaf = kLeaves[li];
-      rc = flg_bvh_set_width(ctx, bvh, w, leaf);
-      if (rc) goto done;
-      for (int stack : {32, 64}) {
-        if (w == 2 && stack == 32) continue;
-        for (int pers : {0, 1, 2}) {
-          if (w == 2 && pers) continue;
-          static const int kRefill[3] = {8, 16, 24};
-          for (int ri = 0; ri < (pers ? 3 : 1); ++ri) {
-            const int refill = pers ? kRefill[ri] : 0;
-            for (int threads : {128, 256}) {
-              flg_trace_opts op{};
-              op.stack_depth = stack;
-              op.persistent = pers;
-              op.refill_lanes = refill ? refill : 16;
-              op.block_threads = threads;
-              // warm-up + 3 timed runs, median-free mean
-              rc = trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, &op, nullptr, 1, &h, nullptr);
-              if (rc) goto done;
-              cudaEventRecord(e0, ctx->stream);
-              for (int r = 0; r < 3 && !rc; ++r)
-                rc = trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, &op, nullptr, 1, &h, nullptr);
-              if (rc) goto done;
-              cudaEventRecord(e1, ctx->stream);
-              cudaEventSynchronize(e1);
-              float ms = 0.0f;
-              cudaEventElapsedTime(&ms, e0, e1);
-              ms /= 3.0f;
-              char line[256];
-              snprintf(line, sizeof(line),
-                       "%s{\"node_width\": %d, \"leaf_size\": %d, \"stack_depth\": %d, \"persistent\": %d, "
-                       "\"refill_lanes\": %d, \"block_threads\": %d, \"ms\": %.5f, \"mrays_s\": %.2f}",
-                       first ? "" : ", ", w, leaf, stack, pers, op.refill_lanes, threads, ms,
-                       n / (ms * 1e3));
-              first = false;
-              rec += line;
-              if (ms < best_ms) {
-                best_ms = ms;
-                bo = op;
-                bw = w;
-                bl = leaf;
-              }
-            }
-          }
-        }
-      }
-    }
+  if (ctx->ray_off_cap < ns + 1) {
+    cudaFree(ctx->d_ray_off);
+    ctx->d_ray_off = nullptr;
+    ctx->ray_off_cap = 0;
+    FLG_CUDA(ctx, cudaMalloc((void **)&ctx->d_ray_off, sizeof(int64_t) * (ns + 1)));
+    ctx->ray_off_cap = ns + 1;
   }
-  {
-    int best_leaf = bl;
-    rc = flg_bvh_set_width(ctx, bvh, bw, best_leaf);
-    if (rc) goto done;
-    // The ray-sort key, tried on the best layout: it pays when neighbouring
-    // rays are scattered, costs a sort and two gathers when they are not.
-    flg_trace_opts op = bo;
-    op.ray_sort = 1;
-    rc = trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, &op, nullptr, 1, &h, nullptr);
-    if (rc) goto done;
-    cudaEventRecord(e0, ctx->stream);
-    for (int r = 0; r < 3 && !rc; ++r) rc = trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, &op, nullptr, 1, &h, nullptr);
-    if (rc) goto done;
-    cudaEventRecord(e1, ctx->stream);
-    cudaEventSynchronize(e1);
-    float ms = 0.0f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    ms /= 3.0f;
-    char line[160];
-    snprintf(line, sizeof(line), ", {\"ray_sort\": 1, \"on_best\": true, \"ms\": %.5f, \"mrays_s\": %.2f}", ms,
-             n / (ms * 1e3));
-    rec += line;
-    if (ms < best_ms) {
-      best_ms = ms;
-      bo = op;
-    }
-    char tail[288];
-    snprintf(tail, sizeof(tail),
-             "], \"best\": {\"node_width\": %d, \"leaf_size\": %d, \"stack_depth\": %d, \"persistent\": %d, "
-             "\"refill_lanes\": %d, \"block_threads\": %d, \"ray_sort\": %d, \"ms\": %.5f}}",
-             bw, best_leaf, bo.stack_depth, bo.persistent, bo.refill_lanes, bo.block_threads, bo.ray_sort, best_ms);
-    rec += tail;
-  }
-done:
-  (void)orig_w;
-  (void)orig_leaf;
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaFree(buf);
-  if (rc) return rc;
-  *best = bo;
-  if (best_width) *best_width = bw;
-  if (json && json_len) {
-    std::strncpy(json, rec.c_str(), json_len - 1);
-    json[json_len - 1] = '\0';
-  }
-  return flg_ctx_sync(ctx);
+  FLG_CUDA(ctx, cudaMemcpy(ctx->d_ray_off, ray_offsets_host, sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice));
+  ctx->ray_off_h.assign(ray_offsets_host, ray_offsets_host + ns + 1);
+  return autotune(ctx, bvh, rays, n, ctx->d_ray_off, ns, reps, best, best_width, best_leaf, json, json_len);
 }
 
 // ---------------------------------------------------------------------------

@@ -236,17 +236,47 @@ FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *ray
 FLG_API int flg_trace_closest_noalloc(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n,
                                       flg_hits *out);
 
-/* Sweeps node width (2/4/8) with leaf ranges of 1/2/3/4 triangles, stack
- * depth (32/64), persistent kernel on/off with refill thresholds and ray
- * sorting on the given workload; leaves the handle laid out at the fastest
- * width and leaf size, returns the fastest options in *best and writes a JSON
- * record (NUL-terminated) to json_out. */
+/* Autotuner of the traversal (no counterpart in the reference): a staged
+ * search on the given workload — (1) node width 2/4/8 with leaf ranges of
+ * 1..4 triangles under each width's default kernel, (2) on the fastest
+ * layout the kernel (one ray per thread, persistent, persistent while-while;
+ * refill threshold 4/8/16; stack depth 32/64), (3) 128- or 256-thread
+ * blocks, (4) for single-scene traces the ray-sort key.  Each trial is one
+ * untimed and `reps` timed launches; its time is their median.  Leaves the
+ * handle laid out at the fastest width and leaf size, returns the fastest
+ * options in *best and writes a JSON record of every trial (NUL-terminated)
+ * to json_out (FLG_ERR_ARG if json_len is too small).  Synchronous; not
+ * capturable.  flg_autotune_trace: single-scene handles, reps = 5. */
 FLG_API int flg_autotune_trace(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n,
                                flg_trace_opts *best, int32_t *best_node_width, char *json_out,
                                size_t json_len);
+/* The same search over a batched handle and its rays (ray_offsets_host as in
+ * flg_trace_closest_batched); reps in [1, 64]; also returns the leaf size. */
+FLG_API int flg_autotune_trace_batched(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays,
+                                       const int64_t *ray_offsets_host, int32_t reps, flg_trace_opts *best,
+                                       int32_t *best_node_width, int32_t *best_leaf, char *json_out,
+                                       size_t json_len);
 
 /* Re-lays out the traversal nodes of a built handle at another width. */
 FLG_API int flg_bvh_set_width(flg_ctx ctx, flg_bvh bvh, int32_t node_width, int32_t leaf_size);
+
+/* Normals of fixed hits of a single-scene handle, for the interfaces that
+ * return them with the hit (3 n floats, xyz interleaved; zeros where
+ * prim < 0):
+ *   FLG_NORMAL_PLUECKER: BVHRayHit::hit_ng (= hit_ns) of
+ *     RadixBVHBuilder::intersect (radix_bvh.cpp:229-233): the Pluecker
+ *     test's StableTriangleNormal of the ray-relative edges
+ *     (intersector.hpp:44-60, 86-88), normalised with the Euclidean norm in
+ *     double.  The reference's StableNormalize (common/vector.h:495-503) adds
+ *     z instead of z*z; its normals are not unit vectors and it misses the
+ *     triangles for which that sum is negative.
+ *   FLG_NORMAL_GEOMETRIC: SInteraction::m_ng of the live renderer's
+ *     Triangle::intersect (shape.cpp:141): normalize(cross(p1 - p0, p2 - p0))
+ *     in fp32 with the reference's operation order.
+ * rays: origins are read for FLG_NORMAL_PLUECKER; prim: device, n ids. */
+enum { FLG_NORMAL_PLUECKER = 0, FLG_NORMAL_GEOMETRIC = 1 };
+FLG_API int flg_hit_normals(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n, const int32_t *prim,
+                            int32_t kind, float *ng);
 
 /* -------------------------------- adjoint ------------------------------- */
 

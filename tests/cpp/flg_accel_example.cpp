@@ -1,10 +1,12 @@
 // Example caller of the C++ adapters (include/flg_accel.hpp): builds a BVH
 // over a triangle soup read from a binary file, traces host BVHRayHit records
-// (BVHBuilderBase::intersect shape) and writes prim/t/u/v to a binary file.
+// (BVHBuilderBase::intersect shape) and writes prim/t/u/v/hit_ng to a binary
+// file (hit_ns must equal hit_ng, as in the reference; else exit 6).
 // Usage: flg_accel_example <tris.bin> <rays.bin> <out.bin>
 //   tris.bin: int64 n_tri, then 9*n_tri float32
 //   rays.bin: int64 n, then 8*n float32 (ox oy oz dx dy dz tnear tfar, SoA)
-//   out.bin:  n int32 prim, then 3*n float32 (t, u, v)
+//   out.bin:  n int32 prim, then 3*n float32 (t, u, v), then 3*n float32
+//             hit_ng (xyz per ray)
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -51,16 +53,21 @@ int main(int argc, char **argv) {
     }
     bvh.intersect(rh.data(), n);
     std::vector<int32_t> prim(n);
-    std::vector<float> tuv(3 * n);
+    std::vector<float> tuv(3 * n), ng(3 * n);
     for (int64_t i = 0; i < n; ++i) {
       prim[i] = rh[i].prim;
       tuv[i] = rh[i].tfar;
       tuv[n + i] = rh[i].u;
       tuv[2 * n + i] = rh[i].v;
+      for (int k = 0; k < 3; ++k) {
+        ng[3 * i + k] = rh[i].hit_ng[k];
+        if (rh[i].hit_ns[k] != rh[i].hit_ng[k]) return 6;
+      }
     }
     FILE *f = std::fopen(argv[3], "wb");
     std::fwrite(prim.data(), sizeof(int32_t), n, f);
     std::fwrite(tuv.data(), sizeof(float), 3 * n, f);
+    std::fwrite(ng.data(), sizeof(float), 3 * n, f);
     std::fclose(f);
     cudaFree(d_pos);
   } catch (const flg::Error &e) {
