@@ -286,9 +286,17 @@ def topology_mismatch(gpu: dict, ref: dict) -> int:
 # ---------------------------------------------------------------------------
 
 def load_tuned() -> dict:
-    if os.path.exists(TUNED):
-        return json.load(open(TUNED))
-    return {}
+    """The LBVH entry of the committed autotuner record (fledge_gb300/autotune.py):
+    node width, leaf size and trace options, plus what the tuner found for
+    the other builders."""
+    if not os.path.exists(TUNED):
+        return {}
+    rec = json.load(open(TUNED))
+    lb = rec["per_builder"]["lbvh"]
+    return {"node_width": lb["node_width"], "leaf_size": lb["leaf_size"], **lb["trace_opts"],
+            "record": {"fastest_builder": rec["builder"], "reps": rec["reps"], "when": rec["when"],
+                       "search_rays": rec["workload"]["search_rays"],
+                       "step_ms": {k: v["step_ms"] for k, v in rec["per_builder"].items()}}}
 
 
 def run_ours(args, rank: int, world: int, local_rank: int) -> None:
@@ -338,7 +346,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     leaf = args.leaf or tuned.get("leaf_size", 3)
     topts = dict(persistent=args.persistent if args.persistent is not None else tuned.get("persistent", 2),
                  refill_lanes=args.refill or tuned.get("refill_lanes", 8),
-                 stack_depth=args.stack or tuned.get("stack_depth", 64))
+                 stack_depth=args.stack or tuned.get("stack_depth", 64),
+                 block_threads=tuned.get("block_threads", 256))
     bb = F.BatchedRadixBVHBuilder(mesh, offs, ctx, node_width=width, leaf_size=leaf)
     log('first build')
     bb.build()
@@ -590,6 +599,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                                        "triangles, 64 rays/triangle; segmented LBVH build + persistent trace",
                            "triangles": n_tri, "rays": n_rays, "node_width": width, "leaf_size": leaf,
                            "trace_opts": topts, "tuned_from": (TUNED[len(ROOT) + 1:] if tuned else None),
+                           "autotuner": tuned.get("record"),
                            "l2": "inputs larger than L2 (no flush)", "parallelism": f"scene shards x{world}"},
                 "build_ms": round(b_ms, 3), "trace_ms": round(statistics.median(trace_ms), 3),
                 "trace_stages_ms": trace_stages, "hit_rate": round(hit_rate, 4),

@@ -459,11 +459,14 @@ def hit_adjoint(ctx: Context, mesh: InternalTriangleMesh, rays: Rays, hits, dLdt
 def pathtrace(ctx: Context, bvh: RadixBVHBuilder, light_first: int, light_count: int, light_le=(10.0, 10.0, 10.0),
               albedo=(0.7, 0.7, 0.7), eye=(0.0, 0.5, 4.0), target=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0),
               fov_deg: float = 40.0, width: int = 1920, height: int = 1080, spp: int = 16, max_depth: int = 5,
-              volume: Optional["DenseGridVolume"] = None, seed: int = 0, **opts):
+              volume: Optional["DenseGridVolume"] = None, seed: int = 0, mesh_medium: Optional[dict] = None,
+              **opts):
     """Wavefront path tracing of the mesh of `bvh` (PathIntegrator::Li with
     next-event estimation; with `volume`, VolPathIntegrator::Li with the
-    grid's medium filling its box).  Returns (radiance [height, width, 3],
-    stats)."""
+    grid's medium filling its box; with `mesh_medium` = dict(first, count,
+    sigma_s, sigma_a, g, density), VolPathIntegrator::Li with a homogeneous
+    medium bounded by triangles [first, first + count)).  Returns
+    (radiance [height, width, 3], stats)."""
     torch = _torch()
     mesh = bvh.mesh
     sc = _lib.FlgPtScene(_ptr(mesh.p), _ptr(mesh.ind), mesh.n_tri, mesh.n_vert, light_first, light_count,
@@ -473,7 +476,13 @@ def pathtrace(ctx: Context, bvh: RadixBVHBuilder, light_first: int, light_count:
     out = torch.empty((height, width, 3), dtype=torch.float32, device=mesh.p.device)
     st = _lib.FlgPtStats()
     op = _trace_opts(**opts)
-    if volume is None:
+    if mesh_medium is not None:
+        m = mesh_medium
+        mm = _lib.FlgMeshMedium(m["first"], m["count"], (C.c_float * 3)(*m["sigma_s"]),
+                                (C.c_float * 3)(*m["sigma_a"]), m["g"], m.get("density", 1.0))
+        ctx.check(ctx.lib.flg_volpath_mesh(ctx.h, bvh.h, C.byref(mm), seed, C.byref(sc), C.byref(cam), spp,
+                                           max_depth, C.byref(op), C.c_void_p(_ptr(out)), C.byref(st)))
+    elif volume is None:
         ctx.check(ctx.lib.flg_pathtrace(ctx.h, bvh.h, C.byref(sc), C.byref(cam), spp, max_depth, C.byref(op),
                                         C.c_void_p(_ptr(out)), C.byref(st)))
     else:

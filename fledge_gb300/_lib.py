@@ -75,6 +75,11 @@ class FlgPtCamera(C.Structure):
                 ("width", C.c_int32), ("height", C.c_int32)]
 
 
+class FlgMeshMedium(C.Structure):
+    _fields_ = [("first", C.c_int32), ("count", C.c_int32), ("sigma_s", C.c_float * 3), ("sigma_a", C.c_float * 3),
+                ("g", C.c_float), ("density", C.c_float)]
+
+
 class FlgPtStats(C.Structure):
     _fields_ = [("closest_rays", C.c_int64), ("shadow_rays", C.c_int64)]
 
@@ -125,6 +130,8 @@ SIGNATURES = {
                       C.POINTER(FlgPtStats)],
     "flg_volpath": [P, P, P, C.c_uint64, C.POINTER(FlgPtScene), C.POINTER(FlgPtCamera), I32, I32,
                     C.POINTER(FlgTraceOpts), P, C.POINTER(FlgPtStats)],
+    "flg_volpath_mesh": [P, P, C.POINTER(FlgMeshMedium), C.c_uint64, C.POINTER(FlgPtScene), C.POINTER(FlgPtCamera),
+                         I32, I32, C.POINTER(FlgTraceOpts), P, C.POINTER(FlgPtStats)],
     "flg_graph_begin": [P],
     "flg_graph_end": [P, PP],
     "flg_graph_launch": [P, P],

@@ -15,6 +15,17 @@
 //   trace         any hit over the shadow queue; k_pt_shadow adds the
 //                 unoccluded contributions to the image
 //
+// With a medium bounded by a closed mesh (flg_volpath_mesh: the reference's
+// HVolume attached to a mesh primitive, scene.cpp:224-228) the boundary
+// triangles carry no material: a path that reaches one passes straight
+// through (not a bounce) and is inside the medium afterwards if it entered
+// (dot(d, ng) < 0) — SInteraction::SpawnRay's rule (interaction.cpp:16-38),
+// which also puts every ray leaving a material surface outside any medium.
+// Inside, HVolume::sample (volume.cpp:164-190) picks a scattering distance;
+// shadow rays follow VolEstimateTr (integrator.cpp:40-66): closest hits in
+// turn, a material surface blocks, an interface multiplies HVolume::tr of the
+// segment and switches the medium.  Tracking draws come from Philox streams.
+//
 // Emitters are triangles of the mesh.  The reference cannot sample a
 // triangle light (Triangle::sample is TODO, shape.cpp:157-160); here a light
 // triangle is chosen uniformly and a point on it by UniformSampleTriangle
@@ -92,12 +103,26 @@ struct PtScene {
   float eye[3], fwd[3], right[3], up[3];
   float fov_ratio, aspect;
   int width, height, spp, max_depth;
-  // Participating medium filling the grid's box (volumetric path tracing).
+  // Participating medium: 0 none, 1 the grid's medium filling its box,
+  // 2 a homogeneous medium bounded by the interface triangles
+  // [iface_first, iface_first + iface_count).
   int medium;
   GridDev G;
   float g;
   uint64_t seed;
+  int32_t iface_first, iface_count;
+  float msig_s[3], msig_t[3], mdens;
 };
+
+__device__ __forceinline__ bool pt_iface(const PtScene &S, int64_t tri) {
+  return tri >= S.iface_first && tri < S.iface_first + S.iface_count;
+}
+
+// HVolume::tr (volume.cpp:159-161) over [0, t]: exp(-t density sigma_t).
+__device__ __forceinline__ float3 hvol_tr(const PtScene &S, float t) {
+  return make_float3(expf(-t * S.mdens * S.msig_t[0]), expf(-t * S.mdens * S.msig_t[1]),
+                     expf(-t * S.mdens * S.msig_t[2]));
+}
 
 __device__ __forceinline__ float3 pt_vertex(const PtScene &S, int64_t tri, int k) {
   const int64_t v = S.idx ? (int64_t)S.idx[3 * tri + k] : 3 * tri + k;
@@ -142,8 +167,18 @@ struct PtQueues {
   float *rad;                // 3 per path: the path's radiance (each path adds to its own, no atomics)
   int32_t *cnt;              // Halton dimensions consumed, per path
   int32_t *cnt_end;          // dimension count at the end of sample 0, per pixel
-  int32_t *counts;           // [0] queue B size, [1] shadow size
+  int32_t *counts;           // [0] queue B size, [1] shadow size, [2] second shadow queue size
   int32_t n_pix;             // pixels per sample
+  // Medium bounded by a mesh: per path the bounce count, the segment count
+  // (the key of its tracking streams) and whether it is inside; per shadow
+  // slot whether it is inside, and a second shadow queue for the segments
+  // past an interface.
+  int32_t *bnc, *seg;
+  uint8_t *inmed;
+  uint8_t *smed[2];
+  float *sx2[7];
+  float *scontrib2;
+  int32_t *spath2;
 };
 
 __global__ void k_pt_camera(PtScene S, Halton H, int s0, int n_path, PtQueues Q, int qa) {
@@ -178,6 +213,11 @@ __global__ void k_pt_camera(PtScene S, Halton H, int s0, int n_path, PtQueues Q,
   Q.beta[3 * p] = Q.beta[3 * p + 1] = Q.beta[3 * p + 2] = 1.0f;
   Q.rad[3 * p] = Q.rad[3 * p + 1] = Q.rad[3 * p + 2] = 0.0f;
   Q.cnt[p] = cnt;
+  if (S.medium == 2) {  // camera rays start outside any medium
+    Q.bnc[p] = 0;
+    Q.seg[p] = 0;
+    Q.inmed[p] = 0;
+  }
 }
 
 // Warp-aggregated slot in a compacted queue.
@@ -213,6 +253,9 @@ __global__ void __launch_bounds__(256, 4)
   float3 so = o, sd = o, contrib = o, nd = o, no = o;
   float smax = 0.0f;
   const float inv_spp = 1.0f / (float)S.spp;
+  const bool meshmed = S.medium == 2;
+  int bnc = depth, sg = depth;     // bounces and segments so far (equal without interfaces)
+  bool inmed = false, nmed = false, smed = false;  // inside now / after this vertex / shadow ray start
   if (valid) {
     pid = Q.path[qa][q];
     pix = pid % Q.n_pix;
@@ -221,6 +264,11 @@ __global__ void __launch_bounds__(256, 4)
     d = make_float3(Q.rx[qa][3][q], Q.rx[qa][4][q], Q.rx[qa][5][q]);
     beta = make_float3(Q.beta[3 * pid], Q.beta[3 * pid + 1], Q.beta[3 * pid + 2]);
     cnt = Q.cnt[pid];
+    if (meshmed) {
+      bnc = Q.bnc[pid];
+      sg = Q.seg[pid];
+      inmed = Q.inmed[pid] != 0;
+    }
     const int32_t h = prim[q];
     const int x = pix % S.width, y = pix / S.width;
     const uint64_t off = halton_pixel_offset(H, x, y);
@@ -233,17 +281,17 @@ __global__ void __launch_bounds__(256, 4)
       const float3 ng = f3norm(f3cross(f3sub(b, a), f3sub(c, a)));
       const bool is_light = h >= S.light_first && h < S.light_first + S.light_count;
       // emission seen directly (bounces == 0); AreaLight::L (light.cpp:76-79)
-      if (depth == 0 && is_light && f3dot(ng, make_float3(-d.x, -d.y, -d.z)) > 0.0f) {
+      if (bnc == 0 && is_light && f3dot(ng, make_float3(-d.x, -d.y, -d.z)) > 0.0f) {
         Q.rad[3 * pid] += beta.x * S.le[0] * inv_spp;
         Q.rad[3 * pid + 1] += beta.y * S.le[1] * inv_spp;
         Q.rad[3 * pid + 2] += beta.z * S.le[2] * inv_spp;
       }
-      if (depth < S.max_depth) {
+      if (bnc < S.max_depth) {
         const float3 wo = make_float3(-d.x, -d.y, -d.z);
         // Volume::sample over the segment up to the surface (volume.cpp:109-148)
         bool scatter = false;
         float3 ps = p;
-        if (S.medium) {
+        if (S.medium == 1) {
           RayStream rs;
           rs.init(S.seed, path_stream_id(pix, s, depth, 0), 0u);
           scatter = S.G.bidx ? delta_track<true>(S.G, __ldg(S.G.params), o, d, th[q], rs, ps)
@@ -252,7 +300,36 @@ __global__ void __launch_bounds__(256, 4)
             const float wgt = S.G.sigma_s / S.G.sigma_t;
             beta = make_float3(beta.x * wgt, beta.y * wgt, beta.z * wgt);
           }
+        } else if (meshmed && inmed) {
+          // HVolume::sample (volume.cpp:164-190) with ray.m_tMax = t_hit: a
+          // channel, then a distance with pdf sigma_t[ch] e^(-sigma_t[ch] t)
+          RayStream rs;
+          rs.init(S.seed, path_stream_id(pix, s, sg, 0), 0u);
+          const int ch = min((int)((double)rs.next() * 3.0), 2);  // get1D() * 3.0 is a double product
+          const float t = -flg_logf(1.0f - rs.next()) / (S.mdens * S.msig_t[ch]);
+          const float tmax = th[q];
+          const float3 tr = hvol_tr(S, fminf(t, tmax));
+          if (t < tmax) {
+            const float pdf = (S.msig_t[0] * tr.x + S.msig_t[1] * tr.y + S.msig_t[2] * tr.z) * 1.0f / 3.0f;
+            beta = make_float3(beta.x * (S.msig_s[0] * tr.x / pdf), beta.y * (S.msig_s[1] * tr.y / pdf),
+                               beta.z * (S.msig_s[2] * tr.z / pdf));
+            ps = make_float3(o.x + d.x * t, o.y + d.y * t, o.z + d.z * t);
+            scatter = true;
+          } else {
+            const float pdf = (tr.x + tr.y + tr.z) * 1.0f / 3.0f;
+            beta = make_float3(beta.x * (tr.x / pdf), beta.y * (tr.y / pdf), beta.z * (tr.z / pdf));
+          }
         }
+        if (meshmed && !scatter && pt_iface(S, h)) {
+          // a material-less boundary: straight on, not a bounce
+          no = offset_origin(p, ng, d);
+          nd = d;
+          nmed = f3dot(d, ng) < 0.0f;
+          cont = true;
+        } else {
+        nmed = meshmed && scatter && inmed;  // a medium vertex keeps the medium; a surface leaves it
+        smed = nmed;
+        ++bnc;
         // UniformSampleOneLight / EstimateDirect
         const float ul = halton(H, index, cnt);
         const float ua = halton(H, index, cnt + 1), ub = halton(H, index, cnt + 2);
@@ -333,6 +410,7 @@ __global__ void __launch_bounds__(256, 4)
             cont = true;
           }
         }
+        }
       }
     }
     if (!cont && s == 0) Q.cnt_end[pix] = cnt;
@@ -354,6 +432,7 @@ __global__ void __launch_bounds__(256, 4)
     Q.scontrib[3 * ss + 1] = contrib.y;
     Q.scontrib[3 * ss + 2] = contrib.z;
     Q.spath[ss] = pid;
+    if (meshmed) Q.smed[0][ss] = smed ? 1 : 0;
   }
   const int ns = queue_slot(valid && cont, Q.counts);
   if (ns >= 0) {
@@ -364,6 +443,78 @@ __global__ void __launch_bounds__(256, 4)
     Q.beta[3 * pid + 1] = beta.y;
     Q.beta[3 * pid + 2] = beta.z;
     Q.cnt[pid] = cnt;
+    if (meshmed) {
+      Q.bnc[pid] = bnc;
+      Q.seg[pid] = sg + 1;
+      Q.inmed[pid] = nmed ? 1 : 0;
+    }
+  }
+}
+
+// One step of VolEstimateTr (integrator.cpp:40-66) for the shadow rays of a
+// mesh-bounded medium, traced forward with closest hit: no hit within the
+// segment adds the contribution; a material surface blocks; an interface
+// multiplies HVolume::tr of the part travelled if inside, switches the
+// medium as SInteraction::SpawnRay does and queues the rest of the segment
+// from an offset origin.  Contributions carry the transmittance so far.
+__global__ void k_pt_shadow_step(PtScene S, int64_t n, const int32_t *__restrict__ prim, const float *__restrict__ th,
+                                 PtQueues Q, int in) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < n;
+  float *const *sx = in == 0 ? Q.sx : Q.sx2;
+  float *const *so_ = in == 0 ? Q.sx2 : Q.sx;
+  const float *sc = in == 0 ? Q.scontrib : Q.scontrib2;
+  float *sco = in == 0 ? Q.scontrib2 : Q.scontrib;
+  const int32_t *sp = in == 0 ? Q.spath : Q.spath2;
+  int32_t *spo = in == 0 ? Q.spath2 : Q.spath;
+  bool requeue = false;
+  float3 no = make_float3(0.f, 0.f, 0.f), d = no, c = no;
+  float rem = 0.0f;
+  bool nmed = false;
+  int pid = 0;
+  if (valid) {
+    pid = sp[i];
+    c = make_float3(sc[3 * i], sc[3 * i + 1], sc[3 * i + 2]);
+    const int32_t h = prim[i];
+    if (h < 0) {
+      // the light is reached; the last segment is not attenuated (VolEstimateTr
+      // returns tr as it stands when nothing more is hit)
+      Q.rad[3 * pid] += c.x;
+      Q.rad[3 * pid + 1] += c.y;
+      Q.rad[3 * pid + 2] += c.z;
+    } else if (pt_iface(S, h)) {
+      const float t = th[i];
+      if (Q.smed[in][i]) {
+        const float3 tr = hvol_tr(S, t);
+        c = make_float3(c.x * tr.x, c.y * tr.y, c.z * tr.z);
+      }
+      const float3 o = make_float3(sx[0][i], sx[1][i], sx[2][i]);
+      d = make_float3(sx[3][i], sx[4][i], sx[5][i]);
+      rem = sx[6][i] - t;
+      if (rem < 0.0f) {
+        Q.rad[3 * pid] += c.x;
+        Q.rad[3 * pid + 1] += c.y;
+        Q.rad[3 * pid + 2] += c.z;
+      } else {
+        const float3 a = pt_vertex(S, h, 0), b = pt_vertex(S, h, 1), cc = pt_vertex(S, h, 2);
+        const float3 ng = f3norm(f3cross(f3sub(b, a), f3sub(cc, a)));
+        const float3 ph = make_float3(o.x + d.x * t, o.y + d.y * t, o.z + d.z * t);
+        no = offset_origin(ph, ng, d);
+        nmed = f3dot(d, ng) < 0.0f;
+        requeue = true;
+      }
+    }
+  }
+  const int slot = queue_slot(valid && requeue, Q.counts + 2);
+  if (slot >= 0) {
+    so_[0][slot] = no.x; so_[1][slot] = no.y; so_[2][slot] = no.z;
+    so_[3][slot] = d.x; so_[4][slot] = d.y; so_[5][slot] = d.z;
+    so_[6][slot] = rem;
+    sco[3 * slot] = c.x;
+    sco[3 * slot + 1] = c.y;
+    sco[3 * slot + 2] = c.z;
+    spo[slot] = pid;
+    Q.smed[in ^ 1][slot] = nmed ? 1 : 0;
   }
 }
 
@@ -449,9 +600,9 @@ static void host_halton(int width, int height, Halton &H) {
 
 using namespace flg;
 
-static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed, const flg_pt_scene *scene,
-                         const flg_pt_camera *cam, int32_t spp, int32_t max_depth, const flg_trace_opts *opts,
-                         float *radiance, flg_pt_stats *stats) {
+static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, const flg_mesh_medium *mm, uint64_t seed,
+                         const flg_pt_scene *scene, const flg_pt_camera *cam, int32_t spp, int32_t max_depth,
+                         const flg_trace_opts *opts, float *radiance, flg_pt_stats *stats) {
   if (!ctx || !bvh || !scene || !cam || !radiance) return ctx ? set_error(ctx, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
   if (spp > 65535 || max_depth > 255) return set_error(ctx, FLG_ERR_ARG, "spp above 65535 or depth above 255");
   if (ctx->capturing) return set_error(ctx, FLG_ERR_STATE, "path tracing synchronises per bounce; not capturable");
@@ -462,14 +613,38 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
   if (scene->light_count < 1 || scene->light_first < 0 || scene->light_first + scene->light_count > scene->n_tri)
     return set_error(ctx, FLG_ERR_ARG, "light triangles out of range");
   if ((int64_t)cam->width * cam->height > (int64_t)1 << 26) return set_error(ctx, FLG_ERR_UNSUPPORTED, "image too large");
+  if (mm) {
+    if (mm->first < 0 || mm->count < 1 || (int64_t)mm->first + mm->count > scene->n_tri)
+      return set_error(ctx, FLG_ERR_ARG, "medium boundary triangles out of range");
+    if (mm->first < scene->light_first + scene->light_count && scene->light_first < mm->first + mm->count)
+      return set_error(ctx, FLG_ERR_ARG, "medium boundary and light triangles overlap");
+    for (int k = 0; k < 3; ++k)
+      if (!(mm->sigma_s[k] >= 0.0f) || !(mm->sigma_a[k] >= 0.0f) || !(mm->sigma_s[k] + mm->sigma_a[k] > 0.0f))
+        return set_error(ctx, FLG_ERR_ARG, "medium coefficients must be >= 0 with sigma_t > 0");
+    if (!(mm->density > 0.0f) || !(mm->g > -1.0f && mm->g < 1.0f))
+      return set_error(ctx, FLG_ERR_ARG, "medium density must be > 0 and |g| < 1");
+  }
   PtScene S;
-  S.medium = grid ? 1 : 0;
+  std::memset(&S, 0, sizeof(S));
+  S.medium = grid ? 1 : mm ? 2 : 0;
+  if (mm) {
+    S.iface_first = mm->first;
+    S.iface_count = mm->count;
+    for (int k = 0; k < 3; ++k) {
+      S.msig_s[k] = mm->sigma_s[k];
+      S.msig_t[k] = mm->sigma_s[k] + mm->sigma_a[k];
+    }
+    S.mdens = mm->density;
+    S.g = mm->g;
+  } else {
+    S.iface_first = -1;
+    S.iface_count = 0;
+  }
   if (grid) {
     if (grid->ctx != ctx) return set_error(ctx, FLG_ERR_ARG, "grid belongs to another context");
     S.G = grid_dev(grid);
     S.g = grid->medium.g;
-  } else {
-    std::memset(&S.G, 0, sizeof(S.G));
+  } else if (!mm) {
     S.g = 0.0f;
   }
   S.seed = seed;
@@ -518,8 +693,11 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
   // Buffers (per path slot): 2 x 6 ray arrays, 2 path maps, 7 + 6 shadow
   // arrays + 3 contrib + path, beta 3, radiance 3, cnt, hits 4, occluded; cnt_end per
   // pixel; counters.  Each sub-buffer is rounded up to 256 bytes.
+  // With a mesh-bounded medium also: bounce and segment counts, inside flags
+  // (per path and per slot of both shadow queues), the second shadow queue.
   const size_t fl = sizeof(float) * np;
-  const size_t need = fl * (12 + 2 + 7 + 6 + 3 + 1 + 3 + 3 + 1 + 4) + sizeof(int32_t) * n + np + 64 + 38 * 256;
+  const size_t extra = mm ? fl * (2 + 7 + 3 + 1) + 3 * (size_t)np + 14 * 256 : 0;
+  const size_t need = fl * (12 + 2 + 7 + 6 + 3 + 1 + 3 + 3 + 1 + 4) + sizeof(int32_t) * n + np + 64 + 38 * 256 + extra;
   if (ctx->pt_bytes < need) {
     cudaFree(ctx->pt_buf);
     ctx->pt_buf = nullptr;
@@ -550,6 +728,21 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
   float *hbuf = (float *)take(4 * fl);
   uint8_t *occ = (uint8_t *)take(np);
   Q.counts = (int32_t *)take(64);
+  Q.bnc = Q.seg = nullptr;
+  Q.inmed = Q.smed[0] = Q.smed[1] = nullptr;
+  for (int k = 0; k < 7; ++k) Q.sx2[k] = nullptr;
+  Q.scontrib2 = nullptr;
+  Q.spath2 = nullptr;
+  if (mm) {
+    Q.bnc = (int32_t *)take(fl);
+    Q.seg = (int32_t *)take(fl);
+    Q.inmed = (uint8_t *)take(np);
+    Q.smed[0] = (uint8_t *)take(np);
+    Q.smed[1] = (uint8_t *)take(np);
+    for (int k = 0; k < 7; ++k) Q.sx2[k] = (float *)take(fl);
+    Q.scontrib2 = (float *)take(3 * fl);
+    Q.spath2 = (int32_t *)take(fl);
+  }
   if (bp > (char *)ctx->pt_buf + need) return set_error(ctx, FLG_ERR_STATE, "internal buffer layout");
 
   cudaStream_t st = ctx->stream;
@@ -563,7 +756,11 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
     k_pt_camera<<<(unsigned)ceil_div(n_path, 256), 256, 0, st>>>(S, H, s0, (int)n_path, Q, qa);
     FLG_LAUNCH_CHECK(ctx, "k_pt_camera");
     int64_t n_a = n_path;
-    for (int depth = 0; depth <= max_depth && n_a > 0; ++depth) {
+    // Without interfaces an iteration is a bounce; with them a path may pass
+    // through boundaries between bounces, up to 255 segments in all (the
+    // segment count keys its tracking streams); paths beyond that end.
+    const int iters = mm ? 255 : max_depth + 1;
+    for (int depth = 0; depth < iters && n_a > 0; ++depth) {
       // t > 0 as the live renderer's Triangle::intersect (shape.cpp:100-148)
       flg_rays rr{Q.rx[qa][0], Q.rx[qa][1], Q.rx[qa][2], Q.rx[qa][3], Q.rx[qa][4], Q.rx[qa][5], nullptr, nullptr,
                   1e-30f, 3.402823466e+38f};
@@ -577,7 +774,27 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
       FLG_LAUNCH_CHECK(ctx, "k_pt_shade");
       FLG_CUDA(ctx, cudaMemcpyAsync(counts, Q.counts, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
       FLG_CUDA(ctx, cudaStreamSynchronize(st));
-      if (counts[1] > 0) {
+      if (counts[1] > 0 && mm) {
+        // VolEstimateTr: closest hits along the segment until it is blocked,
+        // reaches the light or has crossed 64 interfaces (then it counts as
+        // blocked)
+        int64_t n_s = counts[1];
+        for (int step = 0, in = 0; step < 64 && n_s > 0; ++step, in ^= 1) {
+          float *const *sx = in == 0 ? Q.sx : Q.sx2;
+          flg_rays sr{sx[0], sx[1], sx[2], sx[3], sx[4], sx[5], nullptr, sx[6], 1e-30f, 0.0f};
+          flg_hits sh{(int32_t *)hbuf, hbuf + np, hbuf + 2 * np, hbuf + 3 * np};
+          rc = trace_enqueue(ctx, st, 0, bvh, &sr, n_s, opts, nullptr, 1, &sh, nullptr);
+          if (rc) return rc;
+          n_shadow += n_s;
+          FLG_CUDA(ctx, cudaMemsetAsync(Q.counts + 2, 0, sizeof(int32_t), st));
+          k_pt_shadow_step<<<(unsigned)ceil_div(n_s, 256), 256, 0, st>>>(S, n_s, sh.prim, sh.t, Q, in);
+          FLG_LAUNCH_CHECK(ctx, "k_pt_shadow_step");
+          int32_t nn = 0;
+          FLG_CUDA(ctx, cudaMemcpyAsync(&nn, Q.counts + 2, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+          FLG_CUDA(ctx, cudaStreamSynchronize(st));
+          n_s = nn;
+        }
+      } else if (counts[1] > 0) {
         flg_rays sr{Q.rsx[0], Q.rsx[1], Q.rsx[2], Q.rsx[3], Q.rsx[4], Q.rsx[5], nullptr, Q.sx[6], 1e-30f, 0.0f};
         rc = trace_enqueue(ctx, st, 0, bvh, &sr, counts[1], opts, nullptr, 1, nullptr, occ);
         if (rc) return rc;
@@ -601,12 +818,19 @@ static int pathtrace_run(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed,
 
 FLG_API int flg_pathtrace(flg_ctx ctx, flg_bvh bvh, const flg_pt_scene *scene, const flg_pt_camera *cam, int32_t spp,
                           int32_t max_depth, const flg_trace_opts *opts, float *radiance, flg_pt_stats *stats) {
-  return pathtrace_run(ctx, bvh, nullptr, 0, scene, cam, spp, max_depth, opts, radiance, stats);
+  return pathtrace_run(ctx, bvh, nullptr, nullptr, 0, scene, cam, spp, max_depth, opts, radiance, stats);
+}
+
+FLG_API int flg_volpath_mesh(flg_ctx ctx, flg_bvh bvh, const flg_mesh_medium *medium, uint64_t seed,
+                             const flg_pt_scene *scene, const flg_pt_camera *cam, int32_t spp, int32_t max_depth,
+                             const flg_trace_opts *opts, float *radiance, flg_pt_stats *stats) {
+  if (!medium) return ctx ? set_error(ctx, FLG_ERR_ARG, "medium is NULL") : FLG_ERR_ARG;
+  return pathtrace_run(ctx, bvh, nullptr, medium, seed, scene, cam, spp, max_depth, opts, radiance, stats);
 }
 
 FLG_API int flg_volpath(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed, const flg_pt_scene *scene,
                         const flg_pt_camera *cam, int32_t spp, int32_t max_depth, const flg_trace_opts *opts,
                         float *radiance, flg_pt_stats *stats) {
   if (!grid) return ctx ? set_error(ctx, FLG_ERR_ARG, "grid is NULL") : FLG_ERR_ARG;
-  return pathtrace_run(ctx, bvh, grid, seed, scene, cam, spp, max_depth, opts, radiance, stats);
+  return pathtrace_run(ctx, bvh, grid, nullptr, seed, scene, cam, spp, max_depth, opts, radiance, stats);
 }

@@ -1323,10 +1323,17 @@ static unsigned long long *g_noalloc_ptr[64] = {};
 
 // Device address of the scratch array on ctx's device.  In host code the
 // array's name is only a host-side stand-in, so the address is looked up
-// once per device with that device current, and cached.
+// once per device with that device current, and cached.  The lookup may load
+// the library's device code, which a stream capture does not allow: a first
+// call on a device inside a capture is refused, as allocating calls are.
 static int noalloc_scratch(flg_ctx ctx, unsigned long long **out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (ctx->device < 0 || ctx->device >= 64) return set_error(ctx, FLG_ERR_UNSUPPORTED, "device index >= 64");
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (!g_noalloc_ptr[ctx->device] &&
+      (ctx->capturing || (cudaStreamIsCapturing(ctx->stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)))
+    return set_error(ctx, FLG_ERR_STATE,
+                     "the first flg_trace_closest_noalloc on a device looks up its scratch; not allowed during capture");
   if (!g_noalloc_ptr[ctx->device]) {
     int prev = 0;
     FLG_CUDA(ctx, cudaGetDevice(&prev));

@@ -231,8 +231,9 @@ FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *ray
  * scratch is a fixed 8 MB device array inside the library, held on every GPU
  * that loads it until exit.  At most 1,048,576 rays per call (larger n:
  * FLG_ERR_ARG).  The first call on a device looks the array up
- * (cudaGetSymbolAddress) and should come before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race. */
+ * (cudaGetSymbolAddress) and must come before any stream capture (inside a
+ * capture it returns FLG_ERR_STATE).  All calls share the array: calls that
+ * overlap on the GPU race. */
 FLG_API int flg_trace_closest_noalloc(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays, int64_t n,
                                       flg_hits *out);
 
@@ -394,6 +395,36 @@ FLG_API int flg_pathtrace(flg_ctx ctx, flg_bvh bvh, const flg_pt_scene *scene, c
 FLG_API int flg_volpath(flg_ctx ctx, flg_bvh bvh, flg_grid grid, uint64_t seed, const flg_pt_scene *scene,
                         const flg_pt_camera *cam, int32_t spp, int32_t max_depth, const flg_trace_opts *opts,
                         float *radiance, flg_pt_stats *stats);
+
+/* A homogeneous medium bounded by a closed mesh: the reference's HVolume
+ * (src/volume.cpp:150-190) attached to a mesh primitive
+ * (src/scene.cpp:224-228).  Triangles [first, first + count) of the scene
+ * are its boundary; they carry no material. */
+typedef struct flg_mesh_medium {
+  int32_t first, count;
+  float sigma_s[3], sigma_a[3];  /* per RGB channel */
+  float g;                       /* Henyey-Greenstein asymmetry, |g| < 1 */
+  float density;                 /* > 0 */
+} flg_mesh_medium;
+
+/* Volumetric path tracing with that medium (VolPathIntegrator::Li,
+ * src/integrator.cpp:407-510): a path that reaches a boundary triangle passes
+ * straight through (not counted as a bounce; the reference would dereference
+ * the missing material there) and is inside afterwards if it entered
+ * (d . ng < 0, ng = (p1 - p0) x (p2 - p0)); a ray leaving any material
+ * surface is outside (SInteraction::SpawnRay, src/interaction.cpp:16-38).
+ * Inside, HVolume::sample picks a channel and a distance; a scattering vertex
+ * takes next-event estimation with the Henyey-Greenstein phase function and
+ * a HGSampleP continuation.  Shadow rays follow VolEstimateTr
+ * (integrator.cpp:40-66): a material surface blocks, a boundary multiplies
+ * HVolume::tr of the segment travelled inside and switches the medium, and
+ * the segment after the last boundary is not attenuated.  Tracking draws
+ * come from Philox streams keyed by seed, pixel, sample, segment and purpose.
+ * Up to 255 segments per path and 64 boundary crossings per shadow ray.
+ * Synchronises once per segment; not capturable. */
+FLG_API int flg_volpath_mesh(flg_ctx ctx, flg_bvh bvh, const flg_mesh_medium *medium, uint64_t seed,
+                             const flg_pt_scene *scene, const flg_pt_camera *cam, int32_t spp, int32_t max_depth,
+                             const flg_trace_opts *opts, float *radiance, flg_pt_stats *stats);
 
 /* ---------------------------- mesh ingestion ---------------------------- */
 

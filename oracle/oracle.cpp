@@ -1552,17 +1552,51 @@ inline uint64_t path_stream_id(int64_t pix, int s, int depth, int purpose) {
 // (:407-510) with the medium filling the grid's box: delta tracking over the
 // segment up to each surface hit, Henyey-Greenstein scattering, shadow rays
 // weighted by ratio tracking (VolEstimateTr, :40-66).
+//
+// With a medium bounded by a mesh (mm_tri = {first, count} of the boundary
+// triangles, mm_coef = sigma_s[3], sigma_a[3], g, density: HVolume attached
+// to a mesh, scene.cpp:224-228): boundary hits pass straight through without
+// counting as a bounce and set the medium by Entering (interaction.cpp:
+// 16-38; a ray leaving a material surface is outside); inside, HVolume::
+// sample (volume.cpp:164-190) over the segment; shadow rays follow
+// VolEstimateTr (integrator.cpp:40-66) with closest hits through the
+// boundaries.  Draws from Philox streams keyed by the path's segment count.
 ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, const int32_t *perm,
                            const int32_t *split, const uint8_t *leaf, const float *nb, int32_t light_first,
                            int32_t light_count, const float *le, const float *albedo, const float *eye,
                            const float *target, const float *up, float fov_deg, int32_t width, int32_t height,
                            int32_t spp, int32_t max_depth, int32_t pixel_stride, float *radiance,
                            int64_t *rays, const float *rho, int32_t gnx, int32_t gny, int32_t gnz,
-                           const float *glo, const float *ghi, const OrcMedium *gm, uint64_t seed) {
+                           const float *glo, const float *ghi, const OrcMedium *gm, uint64_t seed,
+                           const int32_t *mm_tri, const float *mm_coef) {
   Mesh M{pos, idx, n_tri};
   Tree T{n_tri, perm, split, leaf, nb};
   HaltonH H(width, height);
   const bool medium = rho != nullptr;
+  const bool mm = mm_tri != nullptr;
+  const int32_t if_first = mm ? mm_tri[0] : -1, if_count = mm ? mm_tri[1] : 0;
+  float m_s[3] = {0, 0, 0}, m_t[3] = {1, 1, 1}, m_g = 0.0f, m_dens = 1.0f;
+  if (mm) {
+    for (int k = 0; k < 3; ++k) {
+      m_s[k] = mm_coef[k];
+      m_t[k] = mm_coef[k] + mm_coef[3 + k];
+    }
+    m_g = mm_coef[6];
+    m_dens = mm_coef[7];
+  }
+  auto iface = [&](int64_t tri) { return tri >= if_first && tri < if_first + if_count; };
+  auto closest = [&](V3 o, V3 d, float tmax, Best &b) {  // with the GPU's reported t, u, v
+    RayIn r;
+    r.o[0] = o.x; r.o[1] = o.y; r.o[2] = o.z;
+    r.d[0] = d.x; r.d[1] = d.y; r.d[2] = d.z;
+    for (int k = 0; k < 3; ++k) r.inv[k] = 1.0f / r.d[k];
+    r.tmin = 1e-30f;
+    r.tmax = tmax;
+    b = Best{tmax, -1, 0.0f, 0.0f};
+    recursive_intersect(T, M, 0, r, MODE_DEV, b);
+    if (b.prim >= 0) refine_tuv(M.v(b.prim, 0), M.v(b.prim, 1), M.v(b.prim, 2), r.o, r.d, b.tfar, b.u, b.v);
+  };
+  const float g_phase = mm ? m_g : 0.0f;
   Grid G{};
   if (medium) G = make_grid(rho, gnx, gny, gnz, glo, ghi, gm);
   float f[3] = {target[0] - eye[0], target[1] - eye[1], target[2] - eye[2]};
@@ -1607,7 +1641,10 @@ ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, 
       V3 O = v3(eye[0], eye[1], eye[2]);
       V3 D = norm3(v3(f[0] + xo * r[0] + yo * u3[0], f[1] + xo * r[1] + yo * u3[1], f[2] + xo * r[2] + yo * u3[2]));
       float beta[3] = {1.0f, 1.0f, 1.0f};
+      int bnc = 0, seg = 0;
+      bool inmed = false;
       for (int depth = 0;; ++depth) {
+        if (mm && depth >= 255) break;
         RayIn ray;
         ray.o[0] = O.x; ray.o[1] = O.y; ray.o[2] = O.z;
         ray.d[0] = D.x; ray.d[1] = D.y; ray.d[2] = D.z;
@@ -1625,12 +1662,39 @@ ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, 
                         w * a.z + b.u * bb.z + b.v * c.z);
         const V3 ng = norm3(cross(sub(bb, a), sub(c, a)));
         const bool is_light = b.prim >= light_first && b.prim < light_first + light_count;
-        if (depth == 0 && is_light && dot(ng, v3(-D.x, -D.y, -D.z)) > 0.0f)
+        const int bounce = mm ? bnc : depth;
+        if (bounce == 0 && is_light && dot(ng, v3(-D.x, -D.y, -D.z)) > 0.0f)
           for (int k = 0; k < 3; ++k) acc[k] += (double)(beta[k] * le[k] * inv_spp);
-        if (depth >= max_depth) break;
+        if (bounce >= max_depth) break;
         const V3 wo = v3(-D.x, -D.y, -D.z);
         bool scatter = false;
         V3 ps = p;
+        if (mm && inmed) {
+          // HVolume::sample with ray.m_tMax = the hit distance
+          RayStream rs = stream_for(seed, (int64_t)path_stream_id(pix, s, seg, 0));
+          const int ch = std::min((int)((double)rs.next() * 3.0), 2);
+          const float t = -flg_logf(1.0f - rs.next()) / (m_dens * m_t[ch]);
+          const float tm = std::min(t, b.tfar);
+          float tr[3];
+          for (int k = 0; k < 3; ++k) tr[k] = std::exp(-tm * m_dens * m_t[k]);
+          if (t < b.tfar) {
+            const float pdf = (m_t[0] * tr[0] + m_t[1] * tr[1] + m_t[2] * tr[2]) * 1.0f / 3.0f;
+            for (int k = 0; k < 3; ++k) beta[k] = beta[k] * (m_s[k] * tr[k] / pdf);
+            ps = v3(ray.o[0] + ray.d[0] * t, ray.o[1] + ray.d[1] * t, ray.o[2] + ray.d[2] * t);
+            scatter = true;
+          } else {
+            const float pdf = (tr[0] + tr[1] + tr[2]) * 1.0f / 3.0f;
+            for (int k = 0; k < 3; ++k) beta[k] = beta[k] * (tr[k] / pdf);
+          }
+        }
+        if (mm && !scatter && iface(b.prim)) {  // a material-less boundary: straight on
+          O = offset_origin(p, ng, D);
+          inmed = dot(D, ng) < 0.0f;
+          ++seg;
+          continue;
+        }
+        const bool smed = mm && scatter && inmed;
+        ++bnc;
         if (medium) {
           RayStream rs = stream_for(seed, (int64_t)path_stream_id(pix, s, depth, 0));
           float q[3];
@@ -1662,7 +1726,7 @@ ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, 
           const float pdf = dist * dist / (cos_l * area);
           float fv[3];
           if (scatter) {
-            const float ph = hg_p(wi, wo, G.g);
+            const float ph = hg_p(wi, wo, mm ? g_phase : G.g);
             fv[0] = fv[1] = fv[2] = ph;
           } else {
             const float cos_s = std::fabs(dot(wi, ng));
@@ -1671,7 +1735,36 @@ ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, 
           const float kk = inv_spp / (pdf * light_pdf);
           float ct[3];
           for (int k = 0; k < 3; ++k) ct[k] = beta[k] * fv[k] * le[k] * kk;
-          if (ct[0] > 0.0f || ct[1] > 0.0f || ct[2] > 0.0f) {
+          if ((ct[0] > 0.0f || ct[1] > 0.0f || ct[2] > 0.0f) && mm) {
+            // VolEstimateTr: closest hits through the boundaries
+            V3 so = scatter ? ps : offset_origin(p, ng, wi);
+            float rem = dist - 1e-4f;
+            bool sm = smed;
+            for (int step = 0; step < 64; ++step) {
+              Best hb;
+              closest(so, wi, rem, hb);
+              ++n_shadow;
+              if (hb.prim < 0) {
+                for (int q = 0; q < 3; ++q) acc[q] += (double)ct[q];
+                break;
+              }
+              if (!iface(hb.prim)) break;  // a material surface blocks
+              const float t = hb.tfar;
+              if (sm)
+                for (int q = 0; q < 3; ++q) ct[q] = ct[q] * std::exp(-t * m_dens * m_t[q]);
+              const float rem2 = rem - t;
+              if (rem2 < 0.0f) {
+                for (int q = 0; q < 3; ++q) acc[q] += (double)ct[q];
+                break;
+              }
+              const V3 ia = ld3(M.v(hb.prim, 0)), ib = ld3(M.v(hb.prim, 1)), ic = ld3(M.v(hb.prim, 2));
+              const V3 ing = norm3(cross(sub(ib, ia), sub(ic, ia)));
+              const V3 ph = v3(so.x + wi.x * t, so.y + wi.y * t, so.z + wi.z * t);
+              so = offset_origin(ph, ing, wi);
+              sm = dot(wi, ing) < 0.0f;
+              rem = rem2;
+            }
+          } else if (ct[0] > 0.0f || ct[1] > 0.0f || ct[2] > 0.0f) {
             const V3 so = scatter ? ps : offset_origin(p, ng, wi);
             RayIn sr;
             sr.o[0] = so.x; sr.o[1] = so.y; sr.o[2] = so.z;
@@ -1693,11 +1786,13 @@ ORC_API void orc_pathtrace(const float *pos, const int32_t *idx, int64_t n_tri, 
         }
         const float u1 = H.sample(index, cnt), u2 = H.sample(index, cnt + 1);
         cnt += 2;
+        ++seg;
         if (scatter) {
-          D = hg_sample(wo, u1, u2, G.g);
+          D = hg_sample(wo, u1, u2, mm ? g_phase : G.g);
           O = ps;
-          continue;
+          continue;  // a medium vertex keeps the medium
         }
+        inmed = false;  // a ray leaving a material surface is outside
         V3 bn = std::fabs(ng.x) > std::fabs(ng.z) ? v3(-ng.y, ng.x, 0.0f) : v3(0.0f, -ng.z, ng.y);
         bn = norm3(bn);
         const V3 tg = cross(bn, ng);

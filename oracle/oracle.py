@@ -355,10 +355,12 @@ def num_threads() -> int:
 
 
 def pathtrace(pos, idx, tree, light_first, light_count, le, albedo, eye, target, up, fov_deg, width, height,
-              spp, max_depth, pixel_stride=1, grid=None, seed=0):
+              spp, max_depth, pixel_stride=1, grid=None, seed=0, mesh_medium=None):
     """CPU restatement of the path tracer; returns (radiance [h, w, 3], (closest, shadow) ray counts).
     With pixel_stride > 1 only every pixel_stride-th pixel is rendered.  grid = (rho [nz, ny, nx],
-    lo, hi, Medium) adds the participating medium (volumetric path tracing)."""
+    lo, hi, Medium) adds the participating medium (volumetric path tracing).  mesh_medium =
+    (first, count, sigma_s[3], sigma_a[3], g, density) adds a homogeneous medium bounded by
+    triangles [first, first + count)."""
     pos, idx = _f32(pos), _i32(idx)
     out = np.zeros((height, width, 3), np.float32)
     rays = np.zeros(2, np.int64)
@@ -371,9 +373,17 @@ def pathtrace(pos, idx, tree, light_first, light_count, le, albedo, eye, target,
         gargs = [_p(rho), C.c_int32(nx), C.c_int32(ny), C.c_int32(nz), _p(f3(glo)), _p(f3(ghi)), C.byref(med)]
     else:
         gargs = [None, C.c_int32(0), C.c_int32(0), C.c_int32(0), None, None, None]
+    if mesh_medium is not None:
+        first, count, ss, sa, g, dens = mesh_medium
+        mt = np.array([first, count], np.int32)
+        mc = np.array(list(ss) + list(sa) + [g, dens], np.float32)
+        margs = [_p(mt), _p(mc)]
+    else:
+        margs = [None, None]
     lib().orc_pathtrace(_p(pos), _p(idx), C.c_int64(tree["n"]), _p(_i32(tree["perm"])), _p(_i32(tree["split"])),
                         _p(np.ascontiguousarray(tree["leaf_flags"], np.uint8)), _p(_f32(tree["bounds"])),
                         C.c_int32(light_first), C.c_int32(light_count), *[_p(a) for a in args], C.c_float(fov_deg),
                         C.c_int32(width), C.c_int32(height), C.c_int32(spp), C.c_int32(max_depth),
-                        C.c_int32(pixel_stride), _p(out), _p(rays), *gargs, C.c_uint64(seed))
+                        C.c_int32(pixel_stride), _p(out), _p(rays), *gargs, C.c_uint64(seed),
+                        *margs)
     return out, (int(rays[0]), int(rays[1]))

@@ -100,3 +100,46 @@ def geometric_clusters(n_scales, per_scale, rng):
         tri = c + (rng.uniform(-1.0, 1.0, (per_scale, 3, 3)) * (0.02 * c)).astype(np.float32)
         out.append(tri.astype(np.float32))
     return np.concatenate(out).reshape(-1, 3)
+
+
+def sliver_comb(group, rng):
+    """A scene whose every box is crossed by a bundle of rays that hit
+    nothing but a target at the far end, so that traversal visits every node
+    and its stack grows with the tree's depth.  Slivers along (1, 1, 1) (the
+    third corner within 2^-13 of the axis) with
+    boxes [c - 0.25, c + 0.25]^3 sit at centroids c = 0.5 + e_a 2^j / 1024
+    (axis a, j < 9) and at c = 0.5: the Morton codes of the 28 groups differ in
+    one bit each, a chain 27 levels deep, and each group of `group`
+    equal-code slivers adds a balanced subtree.  Two corner specks fix the
+    scene box to [0, 1]^3.  Returns (positions [n, 3], rays [8, m])."""
+    cents = [np.full(3, 0.5, np.float32)]
+    for a in range(3):
+        for j in range(9):
+            c = np.full(3, 0.5, np.float32)
+            c[a] += np.float32(2.0 ** j / 1024.0)
+            cents.append(c)
+    tris = []
+    eps = np.float32(2.0 ** -12)
+    for c in cents:
+        ang = rng.uniform(0, 2 * np.pi, group)
+        off = np.stack([np.cos(ang), np.sin(ang), -np.cos(ang) - np.sin(ang)], 1).astype(np.float32) * eps * 0.5
+        t = np.empty((group, 3, 3), np.float32)
+        t[:, 0] = c - np.float32(0.25)
+        t[:, 1] = c + np.float32(0.25)
+        t[:, 2] = c + off
+        tris.append(t)
+    speck = np.float32(1e-6)
+    tris.append(np.array([[[0, 0, 0], [speck, 0, 0], [0, speck, 0]],
+                          [[1, 1, 1], [1 - speck, 1, 1], [1, 1 - speck, 1]]], np.float32))
+    # the target: a triangle across the bundle beyond the slivers' boxes' near faces
+    tris.append(np.array([[[0.95, 0.5, 0.5], [0.95, 0.75, 0.5], [0.95, 0.62, 0.75]]], np.float32))
+    pos = np.concatenate(tris).reshape(-1, 3)
+    # rays along +x at y - z = 0.04 +- 0.004: at least 0.0047 from every sliver
+    # axis (where y - z = 0 or +-2^j / 1024), inside every sliver box in y and z
+    m = 4096
+    jit = rng.uniform(-0.002, 0.002, (2, m)).astype(np.float32)
+    r = np.zeros((8, m), np.float32)
+    r[0], r[1], r[2] = 0.0, np.float32(0.62) + jit[0], np.float32(0.58) + jit[1]
+    r[3], r[4], r[5] = 1.0, 0.0, 0.0
+    r[6], r[7] = 0.0, np.inf
+    return pos.astype(np.float32), r

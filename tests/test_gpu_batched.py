@@ -106,6 +106,55 @@ def test_bounded_wait_times_out_and_context_survives(ctx):
     ctx.sync()
 
 
+@pytest.mark.parametrize("batched", [False, True])
+def test_spin_limit_on_real_waits_then_recovers(oracle, batched):
+    """The bounded waits of real multi-tile builds cut to one poll each: the
+    onesweep look-back (a timed-out tile still publishes a prefix), the
+    climb's sibling hand-over (a climb that gives up marks the handle) and the
+    collapse's grid barrier.  Each build returns FLG_OK or FLG_ERR_TIMEOUT,
+    the context stays usable, and the next build with the default limit is
+    bit-exact against the oracle: the marked handle's arrival counters and
+    hand-over records are reset first."""
+    import fledge_gb300 as F
+    from fledge_gb300 import _lib
+    c = F.Context(0)
+    rng = np.random.default_rng(41)
+    counts = [600000] if not batched else [200000, 0, 1, 3072, 150000, 250000]
+    offs = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    pos = G.random_soup(int(offs[-1]), rng)
+    if batched:
+        b = F.BatchedRadixBVHBuilder(F.InternalTriangleMesh(U.dev(pos)), offs, c, node_width=4, leaf_size=3)
+    else:
+        b = F.RadixBVHBuilder(F.InternalTriangleMesh(U.dev(pos)), c, node_width=4, leaf_size=3)
+    b.build()
+    c.sync()
+    status = []
+    c.check(c.lib.flg_ctx_set_spin_limit(c.h, 1))
+    for _ in range(4):
+        b.build()
+        status.append(c.lib.flg_ctx_sync(c.h))
+    c.check(c.lib.flg_ctx_set_spin_limit(c.h, 0))
+    assert set(status) <= {_lib.FLG_OK, _lib.FLG_ERR_TIMEOUT}, status
+    assert _lib.FLG_ERR_TIMEOUT in status, status
+    b.build()
+    c.sync()
+    r8 = G.sphere_rays(1 << 16, np.random.default_rng(42))
+    rd, _ = U.rays_dev(r8)
+    for s, n in enumerate(counts):
+        if n == 0:
+            continue
+        sp = pos[3 * offs[s]:3 * offs[s + 1]]
+        tree = oracle.build_bvh(sp)
+        U.assert_same_topology(b.topology(s) if batched else b.topology(), tree)
+        if not batched:
+            hg = U.host(b.intersect(rd, persistent=2, refill_lanes=8))
+            bad, _, _ = U.compare_closest(oracle, sp, None, tree, r8, hg, oracle.MODE_DEV)
+            assert bad == 0
+    c.sync()
+    b.destroy()
+    c.close()
+
+
 def test_argument_errors_launch_nothing(ctx):
     import fledge_gb300 as F
     from fledge_gb300 import _lib
@@ -127,3 +176,40 @@ def test_argument_errors_launch_nothing(ctx):
     op = F.FlgTraceOpts(48, 0, 0, 0, 0)
     assert ctx.lib.flg_trace_closest(ctx.h, b.h, C.byref(r), 5, C.byref(op), C.byref(hs)) == _lib.FLG_ERR_ARG
     ctx.sync()
+
+
+def test_batched_autotuner_record_and_parity(ctx, oracle):
+    """fledge_gb300.autotune over a batch: every builder searched, the record
+    lists the staged trials with medians, and the winning configuration
+    traces like the oracle."""
+    import fledge_gb300 as F
+    from fledge_gb300 import autotune
+    rng = np.random.default_rng(31)
+    counts = np.round(np.exp(rng.uniform(np.log(500), np.log(60000), 12))).astype(np.int64)
+    bb, pos, soa, offs, roffs = _batch(ctx, counts, rays_per_tri=4)
+    bb.destroy()
+    rays = F.Rays.from_soa(soa, tmin=1e-4)
+    rec = autotune.tune_batched(ctx, F.InternalTriangleMesh(pos), offs, rays, roffs, builders=("lbvh", "sah"),
+                                reps=3, ray_fraction=0.25)
+    assert rec["builder"] in ("lbvh", "sah") and set(rec["per_builder"]) == {"lbvh", "sah"}
+    for name, p in rec["per_builder"].items():
+        stages = {t["stage"] for t in p["search"]["trials"]}
+        assert {"layout", "kernel", "block"} <= stages, name
+        assert all(t["ms_min"] <= t["ms"] <= t["ms_max"] for t in p["search"]["trials"])
+        assert p["search"]["best"]["node_width"] == p["node_width"] and p["search"]["reps"] == 3
+    best = F.BatchedRadixBVHBuilder(F.InternalTriangleMesh(pos), offs, ctx, node_width=rec["node_width"],
+                                    leaf_size=rec["leaf_size"], builder=rec["builder"])
+    best.build()
+    opts = {k: rec[k] for k in ("stack_depth", "block_threads", "persistent", "refill_lanes")}
+    hb = U.host(best.intersect_batched(rays, roffs, **opts))
+    ph, rh = pos.cpu().numpy(), soa.cpu().numpy()
+    for s in (0, 5, 11):
+        sp = ph[3 * offs[s]:3 * offs[s + 1]]
+        r8 = np.zeros((8, roffs[s + 1] - roffs[s]), np.float32)
+        r8[:6] = rh[:, roffs[s]:roffs[s + 1]]
+        r8[6], r8[7] = np.float32(1e-4), np.inf
+        tree = oracle.build_bvh_sah(sp) if rec["builder"] == "sah" else oracle.build_bvh(sp)
+        hs = {k: v[roffs[s]:roffs[s + 1]] for k, v in hb.items()}
+        bad, _, _ = U.compare_closest(oracle, sp, None, tree, r8, hs, oracle.MODE_DEV)
+        assert bad == 0, s
+    best.destroy()
