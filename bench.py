@@ -497,11 +497,11 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         plain["speedup_batched_vs_plain_same_kernel"] = plain["same_kernel"]["speedup_batched_vs_plain"]
         plain["speedup_batched_vs_plain_bvh2"] = plain["bvh2"]["speedup_batched_vs_plain"]
 
-    # ---- high-quality builders (PLOC, binned SAH) on the same scenes and rays ----
-    hq = sah = None
+    # ---- higher-quality builders (PLOC, binned SAH, treelet-restructured LBVH) on the same scenes and rays ----
+    hq = sah = tl = None
     if not args.skip_hq:
         res = {}
-        for name in ("ploc", "sah"):
+        for name in ("ploc", "sah", "treelet"):
             hb = F.BatchedRadixBVHBuilder(mesh, offs, ctx, node_width=width, leaf_size=leaf, builder=name)
             hb.build()
             hb.intersect_batched(rays, roffs, out=hits, **topts)  # warm-up
@@ -514,14 +514,15 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             ev[2].record(stream)
             torch.cuda.synchronize()
             hb_ms, ht_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
-            res[name] = {"builder": "ploc (radius 16)" if name == "ploc" else "binned SAH (16 buckets, reference rule)",
+            res[name] = {"builder": {"ploc": "ploc (radius 16)", "sah": "binned SAH (16 buckets, reference rule)",
+                                     "treelet": "LBVH + 3 rounds of 7-leaf treelet restructuring"}[name],
                          "build_ms": round(hb_ms, 3), "trace_ms": round(ht_ms, 2),
                          "mrays_s": round(n_rays / (ht_ms * 1e-3) / 1e6, 1),
                          "trace_speedup_vs_lbvh": round(statistics.median(trace_ms) / ht_ms, 3),
                          "step_ms": round(hb_ms + ht_ms, 2)}
             hb.destroy()
             log(f'{name} builder done')
-        hq, sah = res["ploc"], res["sah"]
+        hq, sah, tl = res["ploc"], res["sah"], res["treelet"]
 
     # ---- e2e: host (pinned) inputs, copies inside the timed region ----
     e2e = None
@@ -604,7 +605,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                 "build_ms": round(b_ms, 3), "trace_ms": round(statistics.median(trace_ms), 3),
                 "trace_stages_ms": trace_stages, "hit_rate": round(hit_rate, 4),
                 "build_roofline": build_roof, "roofline": roof, "plain": plain, "volume": vol,
-                "hq_builder": hq, "sah_builder": sah, "config0": c0, "config1": c1, "config1_volume": c1v,
+                "hq_builder": hq, "sah_builder": sah, "treelet_builder": tl, "config0": c0, "config1": c1, "config1_volume": c1v,
                 "config4": c4, "parity": parity, "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
                 "gpu_launches": int(launches), "gpu_launches_total": int(total_launches)}
         print(json.dumps(line), flush=True)

@@ -155,9 +155,11 @@ def _trace_opts(stack_depth=0, block_threads=0, persistent=0, refill_lanes=0, ra
 
 
 def _builder_id(name: str) -> int:
-    """'lbvh' (the Karras radix tree), 'ploc' (locally-ordered clustering) or
-    'sah' (BasicBVHBuilder's binned-SAH build)."""
-    ids = {"lbvh": _lib.FLG_BUILDER_LBVH, "ploc": _lib.FLG_BUILDER_PLOC, "sah": _lib.FLG_BUILDER_SAH}
+    """'lbvh' (the Karras radix tree), 'ploc' (locally-ordered clustering),
+    'sah' (BasicBVHBuilder's binned-SAH build) or 'treelet' (the LBVH refined
+    by treelet restructuring)."""
+    ids = {"lbvh": _lib.FLG_BUILDER_LBVH, "ploc": _lib.FLG_BUILDER_PLOC, "sah": _lib.FLG_BUILDER_SAH,
+           "treelet": _lib.FLG_BUILDER_TREELET}
     if name not in ids:
         raise ValueError(f"builder must be one of {sorted(ids)}")
     return ids[name]

@@ -19,7 +19,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libflg.so")
 
 SOURCES = ["api.cu", "build.cu", "sort.cu", "collapse.cu", "trace.cu", "volume.cu",
-           "adjoint.cu", "gen.cu", "pathtrace.cu", "ploc.cu", "sah.cu", "ply.cpp"]
+           "adjoint.cu", "gen.cu", "pathtrace.cu", "ploc.cu", "sah.cu", "treelet.cu", "ply.cpp"]
 HEADERS = [os.path.join(CSRC, "common.cuh"), os.path.join(CSRC, "internal.h"), os.path.join(CSRC, "volume.cuh"),
            os.path.join(ROOT, "include", "flg.h")]
 

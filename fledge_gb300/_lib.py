@@ -31,7 +31,7 @@ class FlgBuildOpts(C.Structure):
                 ("builder", C.c_int32)]
 
 
-FLG_BUILDER_LBVH, FLG_BUILDER_PLOC, FLG_BUILDER_SAH = 0, 1, 2
+FLG_BUILDER_LBVH, FLG_BUILDER_PLOC, FLG_BUILDER_SAH, FLG_BUILDER_TREELET = 0, 1, 2, 3
 
 
 class FlgTraceOpts(C.Structure):

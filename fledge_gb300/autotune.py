@@ -3,7 +3,8 @@ reference): picks the tree builder, the node width and leaf size, and the
 traversal kernel options of a batched workload, and persists the choice as a
 JSON record that the benchmark loads.
 
-For every builder (the Karras LBVH, PLOC, the binned-SAH rule) the batch is
+For every builder (the Karras LBVH, PLOC, the binned-SAH rule, the LBVH
+refined by treelet restructuring) the batch is
 built, the build is timed (median of `reps`), and flg_autotune_trace_batched
 runs its staged search (layout, kernel, block size; each trial the median of
 `reps` launches) on a fraction of every scene's rays.  The builder whose
@@ -55,7 +56,7 @@ def subsample_offsets(ray_offsets, fraction: float):
 
 
 def tune_batched(ctx: Context, mesh: InternalTriangleMesh, tri_offsets, rays: Rays, ray_offsets,
-                 builders=("lbvh", "ploc", "sah"), reps: int = 5, ray_fraction: float = 0.125) -> dict:
+                 builders=("lbvh", "ploc", "sah", "treelet"), reps: int = 5, ray_fraction: float = 0.125) -> dict:
     """Returns the tuning record (see the module docstring)."""
     torch = _torch()
     ro = np.asarray(ray_offsets, np.int64)
@@ -106,7 +107,7 @@ def tune_batched(ctx: Context, mesh: InternalTriangleMesh, tri_offsets, rays: Ra
 
 
 def tune_config3(out: str = DEFAULT_RECORD, reps: int = 5, ray_fraction: float = 0.125,
-                 builders=("lbvh", "ploc", "sah")) -> dict:
+                 builders=("lbvh", "ploc", "sah", "treelet")) -> dict:
     """Tunes the 256-scene batch with the benchmark's seeds and writes the record."""
     torch = _torch()
     from . import gen_rays, gen_triangles
@@ -135,7 +136,7 @@ def main() -> None:
     ap.add_argument("--out", default=DEFAULT_RECORD)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--ray-fraction", type=float, default=0.125)
-    ap.add_argument("--builders", default="lbvh,ploc,sah")
+    ap.add_argument("--builders", default="lbvh,ploc,sah,treelet")
     a = ap.parse_args()
     rec = tune_config3(a.out, a.reps, a.ray_fraction, tuple(a.builders.split(",")))
     print(json.dumps({k: v for k, v in rec.items() if k != "per_builder"}))

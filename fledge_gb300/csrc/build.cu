@@ -512,6 +512,10 @@ int build_enqueue(flg_ctx ctx, flg_bvh b) {
       b->d_tris, ctx->spin_limit, ctx->d_err, b->d_dirty);
   FLG_LAUNCH_CHECK(ctx, "k_climb");
   stage_mark(ctx, st, "climb");
+  if (b->builder == FLG_BUILDER_TREELET) {
+    rc = treelet_build(ctx, b);
+    if (rc) return rc;
+  }
   if (b->width > 2) return collapse_enqueue(ctx, b, b->width, b->leaf_size);
   return FLG_OK;
 }
@@ -538,8 +542,10 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   if (width != 2 && width != 4 && width != 8) return set_error(ctx, FLG_ERR_ARG, "node_width must be 2, 4 or 8");
   if (leaf_size < 1 || leaf_size > 8) return set_error(ctx, FLG_ERR_ARG, "leaf_size must be in [1, 8]");
   const int builder = opts ? opts->builder : FLG_BUILDER_LBVH;
-  if (builder != FLG_BUILDER_LBVH && builder != FLG_BUILDER_PLOC && builder != FLG_BUILDER_SAH)
-    return set_error(ctx, FLG_ERR_ARG, "builder must be FLG_BUILDER_LBVH, FLG_BUILDER_PLOC or FLG_BUILDER_SAH");
+  if (builder != FLG_BUILDER_LBVH && builder != FLG_BUILDER_PLOC && builder != FLG_BUILDER_SAH &&
+      builder != FLG_BUILDER_TREELET)
+    return set_error(ctx, FLG_ERR_ARG,
+                     "builder must be FLG_BUILDER_LBVH, FLG_BUILDER_PLOC, FLG_BUILDER_SAH or FLG_BUILDER_TREELET");
 
   flg_bvh b = new flg_bvh_t();
   b->ctx = ctx;
@@ -608,6 +614,7 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   A(&b->d_tile_ctr, b->n_passes);
   if (rc == FLG_OK && builder == FLG_BUILDER_PLOC) rc = ploc_reserve(b);
   if (rc == FLG_OK && builder == FLG_BUILDER_SAH) rc = sah_reserve(b);
+  if (rc == FLG_OK && builder == FLG_BUILDER_TREELET) rc = treelet_reserve(b);
   if (rc) {
     flg_bvh_destroy(b);
     return rc;

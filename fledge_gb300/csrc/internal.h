@@ -155,6 +155,17 @@ struct flg_bvh_t {
   uint32_t *d_sbins[2] = {nullptr, nullptr};
   int4 *d_sfin = nullptr;
   int32_t *d_sflag = nullptr, *d_sscan = nullptr, *d_ssum = nullptr, *d_sctr = nullptr, *d_sroot = nullptr;
+  // Treelet restructuring (builder == FLG_BUILDER_TREELET): per node slot
+  // children, parent, leaf count, first leaf, Karras slot (6 x int32), per
+  // leaf parent and new position (2 x int32), arrival counters, costs and
+  // boxes; the rewritten node records, triangle records and order.
+  int32_t *d_tl_i32 = nullptr;
+  uint32_t *d_tl_flag = nullptr;
+  float *d_tl_cost = nullptr;
+  float4 *d_tl_box = nullptr;
+  flg::Node2 *d_tl_nodes = nullptr;
+  flg::TriRec *d_tl_tris = nullptr;
+  uint32_t *d_tl_perm = nullptr;
 };
 
 struct flg_grid_t {
@@ -256,6 +267,8 @@ int ploc_reserve(flg_bvh b);
 int ploc_build(flg_ctx ctx, flg_bvh b);
 int sah_reserve(flg_bvh b);
 int sah_build(flg_ctx ctx, flg_bvh b);
+int treelet_reserve(flg_bvh b);
+int treelet_build(flg_ctx ctx, flg_bvh b);
 // Exclusive scan of int32 flags (ploc.cu): per-tile scans and tile sums
 // (kFlagScanThreads threads, kFlagScanTile flags per tile), then a one-CTA
 // (1024 threads) exclusive scan of the tile sums that also writes the total.

@@ -1,0 +1,393 @@
+// treelet.cu — treelet restructuring of the LBVH (FLG_BUILDER_TREELET):
+// Karras & Aila, "Fast Parallel Construction of High-Quality Bounding Volume
+// Hierarchies" (HPG 2013).  No counterpart in the reference, whose quality
+// builder is the binned SAH of base_bvh.cpp:33-173; this is the LBVH
+// refinement that trades build time for trace speed.
+//
+// After the Karras build (k_climb) the node records are turned into a working
+// form (children, parents, leaf counts, boxes, SAH costs).  Each of three
+// rounds is one bottom-up pass with arrival counters, as the refit: the
+// second child to arrive finishes a node (box, count, cost
+// Ci A + C(left) + C(right), A = dx dy + dy dz + dz dx) and, when its
+// subtree holds at least 7 << round triangles, rebuilds the treelet of its 7
+// largest descendants (the treelet leaf of largest area is opened until 7
+// leaves; ties to the first in list order) into the topology of least SAH
+// cost by dynamic programming over the 127 subsets of the treelet's leaves
+// (splits holding the lowest member, enumerated from S - 1 downwards, first
+// minimum kept).  A node is finished only after its subtree, so the result
+// does not depend on scheduling.  Nothing waits: the first arrival stops.
+// Then every node finds its first leaf in depth-first order by climbing to
+// its root, the leaves and triangle records are regathered in that order and
+// the node records are rewritten in Karras' numbering (root at the scene's
+// first slot, a left child at its last position, a right child at its
+// first), so traversal, the wide collapse and flg_bvh_download read the tree
+// as they read an LBVH.  Morton codes no longer follow the leaf order.
+#include "common.cuh"
+#include "internal.h"
+
+namespace flg {
+
+constexpr float kTlCi = 1.2f, kTlCt = 1.0f;
+constexpr int kTreelet = 7, kTlFull = (1 << kTreelet) - 1;
+constexpr int kTlRounds = 3;
+constexpr int kTlThreads = 64;
+
+struct TlBox {
+  float lo[3], hi[3];
+};
+
+__device__ __forceinline__ float tl_area(const TlBox &b) {
+  const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+  return dx * dy + dy * dz + dz * dx;
+}
+__device__ __forceinline__ void tl_merge(TlBox &a, const TlBox &b) {
+  for (int k = 0; k < 3; ++k) {
+    a.lo[k] = fminf(a.lo[k], b.lo[k]);
+    a.hi[k] = fmaxf(a.hi[k], b.hi[k]);
+  }
+}
+
+// Working form: per node slot children (>= 0 node slot, < 0 ~sorted leaf),
+// parent (-1 at a root), leaf count, SAH cost, box; per leaf its parent.
+// Reads of what other threads write go through L2 (__ldcg): L1 is not
+// coherent across SMs.
+struct Tl {
+  int32_t *left, *right, *parent, *nleaf, *first, *slot;
+  uint32_t *flag;
+  float *cost;
+  float4 *box;  // 2 per node: lo.xyz, hi.xyz
+  int32_t *lpar, *lpos;
+  const TriRec *tris;
+
+  __device__ __forceinline__ TlBox leaf_box(int32_t pos) const {
+    const TriRec t = tris[pos];
+    TlBox b;
+    b.lo[0] = fminf(fminf(t.p0.x, t.p1.x), t.p2.x);
+    b.lo[1] = fminf(fminf(t.p0.y, t.p1.y), t.p2.y);
+    b.lo[2] = fminf(fminf(t.p0.z, t.p1.z), t.p2.z);
+    b.hi[0] = fmaxf(fmaxf(t.p0.x, t.p1.x), t.p2.x);
+    b.hi[1] = fmaxf(fmaxf(t.p0.y, t.p1.y), t.p2.y);
+    b.hi[2] = fmaxf(fmaxf(t.p0.z, t.p1.z), t.p2.z);
+    return b;
+  }
+  __device__ __forceinline__ TlBox bx(int32_t r) const {
+    if (r < 0) return leaf_box(~r);
+    const float4 a = __ldcg(box + 2 * r), b = __ldcg(box + 2 * r + 1);
+    TlBox o;
+    o.lo[0] = a.x; o.lo[1] = a.y; o.lo[2] = a.z;
+    o.hi[0] = b.x; o.hi[1] = b.y; o.hi[2] = b.z;
+    return o;
+  }
+  __device__ __forceinline__ float cs(int32_t r) const {
+    return r < 0 ? kTlCt * tl_area(leaf_box(~r)) : __ldcg(cost + r);
+  }
+  __device__ __forceinline__ int32_t nl(int32_t r) const { return r < 0 ? 1 : __ldcg(nleaf + r); }
+  __device__ __forceinline__ void set_parent(int32_t r, int32_t p) const {
+    if (r >= 0) parent[r] = p;
+    else lpar[~r] = p;
+  }
+  __device__ __forceinline__ void store(int32_t x, const TlBox &b, float c, int32_t n) const {
+    box[2 * x] = make_float4(b.lo[0], b.lo[1], b.lo[2], 0.0f);
+    box[2 * x + 1] = make_float4(b.hi[0], b.hi[1], b.hi[2], 0.0f);
+    cost[x] = c;
+    nleaf[x] = n;
+  }
+
+  __device__ void finish(int32_t x) const {
+    const int32_t l = __ldcg(left + x), r = __ldcg(right + x);
+    TlBox b = bx(l);
+    tl_merge(b, bx(r));
+    store(x, b, kTlCi * tl_area(b) + (cs(l) + cs(r)), nl(l) + nl(r));
+  }
+
+  __device__ void restructure(int32_t R) const {
+    int32_t L[kTreelet], I[kTreelet - 1];
+    int nL = 2, nI = 1;
+    L[0] = __ldcg(left + R);
+    L[1] = __ldcg(right + R);
+    I[0] = R;
+    while (nL < kTreelet) {
+      int best = -1;
+      float ba = -1.0f;
+      for (int k = 0; k < nL; ++k)
+        if (L[k] >= 0) {
+          const float a = tl_area(bx(L[k]));
+          if (a > ba) {
+            ba = a;
+            best = k;
+          }
+        }
+      if (best < 0) return;
+      const int32_t x = L[best];
+      I[nI++] = x;
+      L[best] = __ldcg(left + x);
+      L[nL++] = __ldcg(right + x);
+    }
+    TlBox lb[kTreelet];
+    float lc[kTreelet];
+    int32_t ln[kTreelet];
+    for (int k = 0; k < kTreelet; ++k) {
+      lb[k] = bx(L[k]);
+      lc[k] = cs(L[k]);
+      ln[k] = nl(L[k]);
+    }
+    float c[kTlFull + 1];
+    uint8_t part[kTlFull + 1];
+    for (int S = 1; S <= kTlFull; ++S) {
+      const int low = S & -S;
+      if (S == low) {
+        c[S] = lc[__ffs(low) - 1];
+        part[S] = 0;
+        continue;
+      }
+      TlBox u = lb[__ffs(low) - 1];
+      for (int k = 0; k < kTreelet; ++k)
+        if ((S >> k) & 1) tl_merge(u, lb[k]);
+      float best = 3.402823466e+38f;
+      int bp = 0;
+      for (int P = (S - 1) & S; P > 0; P = (P - 1) & S) {
+        if (!(P & low)) continue;
+        const float v = c[P] + c[S ^ P];
+        if (v < best) {
+          best = v;
+          bp = P;
+        }
+      }
+      c[S] = kTlCi * tl_area(u) + best;
+      part[S] = (uint8_t)bp;
+    }
+    // Rebuild: internal nodes taken from I as their parents are expanded
+    // (left child first), expansion by a stack with the left subtree on top.
+    int next = 1, sp = 0, no = 0;
+    int stS[kTreelet];
+    int32_t stN[kTreelet], order[kTreelet - 1];
+    int orderS[kTreelet - 1];
+    stS[sp] = kTlFull;
+    stN[sp++] = R;
+    while (sp) {
+      --sp;
+      const int S = stS[sp];
+      const int32_t node = stN[sp];
+      order[no] = node;
+      orderS[no++] = S;
+      const int P = part[S], Q = S ^ P;
+      const int32_t c0 = __popc(P) == 1 ? L[__ffs(P) - 1] : I[next++];
+      const int32_t c1 = __popc(Q) == 1 ? L[__ffs(Q) - 1] : I[next++];
+      left[node] = c0;
+      right[node] = c1;
+      set_parent(c0, node);
+      set_parent(c1, node);
+      if (__popc(Q) > 1) {
+        stS[sp] = Q;
+        stN[sp++] = c1;
+      }
+      if (__popc(P) > 1) {
+        stS[sp] = P;
+        stN[sp++] = c0;
+      }
+    }
+    // boxes, counts and costs bottom-up (children were expanded later)
+    for (int k = no - 1; k >= 0; --k) {
+      const int S = orderS[k];
+      TlBox u = lb[__ffs(S & -S) - 1];
+      int32_t n = 0;
+      for (int j = 0; j < kTreelet; ++j)
+        if ((S >> j) & 1) {
+          tl_merge(u, lb[j]);
+          n += ln[j];
+        }
+      store(order[k], u, c[S], n);
+    }
+  }
+};
+
+// A child ref of a node of the scene [toff, toff + n): a node slot in
+// [toff, toff + n - 1) or ~position in [toff, toff + n).
+__device__ __forceinline__ bool tl_ref_ok(int32_t r, int64_t toff, int64_t n) {
+  return r >= 0 ? (r >= toff && r < toff + n - 1) : (~r >= toff && ~r < toff + n);
+}
+
+__global__ void __launch_bounds__(256)
+    k_tl_init(const Node2 *__restrict__ nodes, int64_t n_nodes, const int64_t *__restrict__ tri_off, int n_scenes,
+              Tl T, uint32_t *err) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n_nodes;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int s = find_segment(tri_off, n_scenes, g);
+    const int64_t toff = tri_off[s], n = tri_off[s + 1] - toff;
+    if (g >= toff + n - 1) continue;  // a scene's last slot is unused
+    const int4 d = nodes[g].d;
+    T.flag[g] = 0u;
+    // only a build whose bounded waits gave up leaves refs outside the scene
+    if (!tl_ref_ok(d.x, toff, n) || !tl_ref_ok(d.y, toff, n)) {
+      atomicOr(err, kErrTimeout);
+      T.left[g] = T.right[g] = ~(int32_t)toff;
+      continue;
+    }
+    T.left[g] = d.x;
+    T.right[g] = d.y;
+    T.set_parent(d.x, (int32_t)g);
+    T.set_parent(d.y, (int32_t)g);
+  }
+}
+
+// One round: a thread per leaf climbs; the second arrival at a node finishes
+// it (and rebuilds its treelet when its subtree is large enough).
+__global__ void __launch_bounds__(kTlThreads)
+    k_tl_round(int64_t n_tri, int32_t gamma, Tl T) {
+  for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n_tri;
+       pos += (int64_t)gridDim.x * blockDim.x) {
+    int32_t x = __ldcg(T.lpar + pos);
+    // a valid tree is at most 62 levels deep; the bound only matters for a
+    // tree left inconsistent by an earlier timed-out build
+    for (int depth = 0; x >= 0 && depth < 128; ++depth) {
+      __threadfence();
+      if (atomicAdd(T.flag + x, 1u) == 0u) break;
+      T.flag[x] = 0u;  // both arrivals seen: ready for the next round
+      __threadfence();
+      T.finish(x);
+      if (__ldcg(T.nleaf + x) >= gamma) T.restructure(x);
+      __threadfence();
+      x = __ldcg(T.parent + x);
+    }
+  }
+}
+
+// Depth-first position of every node's first leaf (climb to the root adding
+// the left siblings' leaf counts) and the internal nodes' Karras slots.
+__global__ void __launch_bounds__(256)
+    k_tl_first(int64_t n_nodes, int64_t n_tri, const int64_t *__restrict__ tri_off, int n_scenes, Tl T) {
+  const int64_t total = n_nodes + n_tri;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+    const bool leaf = k >= n_nodes;
+    const int64_t g = leaf ? k - n_nodes : k;
+    const int s = find_segment(tri_off, n_scenes, g);
+    const int64_t toff = tri_off[s];
+    if (!leaf && g >= tri_off[s + 1] - 1) continue;
+    int32_t x = leaf ? ~(int32_t)g : (int32_t)g;
+    int32_t p = leaf ? T.lpar[g] : T.parent[g];
+    int64_t f = 0;
+    bool is_left = true;
+    int depth = 0;
+    for (int32_t c = x, q = p; q >= 0 && depth < 128; ++depth) {
+      const bool right = T.right[q] == c;
+      if (c == x) is_left = !right;
+      if (right) f += T.left[q] < 0 ? 1 : T.nleaf[T.left[q]];
+      c = q;
+      q = T.parent[q];
+    }
+    const int64_t n = tri_off[s + 1] - toff;
+    if (leaf) {
+      T.lpos[g] = f < n ? (int32_t)(toff + f) : -1;
+    } else {
+      const int64_t last = f + T.nleaf[g] - 1;
+      const int64_t sl = p < 0 ? 0 : is_left ? last : f;
+      const bool ok = f >= 0 && last < n && sl < n - 1;
+      T.first[g] = ok ? (int32_t)f : -1;
+      T.slot[g] = ok ? (int32_t)(toff + sl) : -1;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_tl_emit(int64_t n_nodes, const int64_t *__restrict__ tri_off, int n_scenes, Tl T, Node2 *__restrict__ out) {
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n_nodes;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int s = find_segment(tri_off, n_scenes, g);
+    const int64_t toff = tri_off[s];
+    if (g >= tri_off[s + 1] - 1) continue;
+    const int32_t l = T.left[g], r = T.right[g];
+    if (T.slot[g] < 0) continue;  // an inconsistent tree (timed-out build): the flagged error stands
+    const TlBox b0 = T.bx(l), b1 = T.bx(r);
+    Node2 nd;
+    nd.a = make_float4(b0.lo[0], b0.hi[0], b0.lo[1], b0.hi[1]);
+    nd.b = make_float4(b1.lo[0], b1.hi[0], b1.lo[1], b1.hi[1]);
+    nd.c = make_float4(b0.lo[2], b0.hi[2], b1.lo[2], b1.hi[2]);
+    const int32_t c0 = l < 0 ? ~T.lpos[~l] : T.slot[l];
+    const int32_t c1 = r < 0 ? ~T.lpos[~r] : T.slot[r];
+    const int32_t f = (int32_t)(toff + T.first[g]);
+    nd.d = make_int4(c0, c1, f, f + T.nleaf[g] - 1);
+    out[T.slot[g]] = nd;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+    k_tl_leaves(int64_t n_tri, Tl T, const uint32_t *__restrict__ perm, uint32_t *__restrict__ perm_out,
+                TriRec *__restrict__ tris_out) {
+  for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n_tri;
+       pos += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t np = T.lpos[pos];
+    if (np < 0 || np >= n_tri) continue;
+    perm_out[np] = perm[pos];
+    tris_out[np] = T.tris[pos];
+  }
+}
+
+static Tl tl_arrays(flg_bvh b) {
+  Tl T;
+  T.left = b->d_tl_i32;
+  T.right = T.left + b->n_nodes;
+  T.parent = T.right + b->n_nodes;
+  T.nleaf = T.parent + b->n_nodes;
+  T.first = T.nleaf + b->n_nodes;
+  T.slot = T.first + b->n_nodes;
+  T.lpar = T.slot + b->n_nodes;
+  T.lpos = T.lpar + b->n_tri;
+  T.flag = b->d_tl_flag;
+  T.cost = b->d_tl_cost;
+  T.box = b->d_tl_box;
+  T.tris = b->d_tris;
+  return T;
+}
+
+int treelet_reserve(flg_bvh b) {
+  int rc = FLG_OK;
+  auto A = [&](auto **p, size_t c) {
+    if (rc == FLG_OK) rc = halloc(b, p, c);
+  };
+  A(&b->d_tl_i32, 6 * (size_t)b->n_nodes + 2 * (size_t)b->n_tri);
+  A(&b->d_tl_flag, b->n_nodes);
+  A(&b->d_tl_cost, b->n_nodes);
+  A(&b->d_tl_box, 2 * (size_t)b->n_nodes);
+  A(&b->d_tl_nodes, b->n_nodes);
+  A(&b->d_tl_tris, b->n_tri);
+  A(&b->d_tl_perm, b->n_tri);
+  return rc;
+}
+
+int treelet_build(flg_ctx ctx, flg_bvh b) {
+  cudaStream_t st = ctx->stream;
+  const int64_t n = b->n_tri, nn = b->n_nodes;
+  if (n <= 1) return FLG_OK;
+  Tl T = tl_arrays(b);
+  // parents of roots (and of one-triangle scenes' leaves) stay -1
+  FLG_CUDA(ctx, cudaMemsetAsync(T.parent, 0xFF, sizeof(int32_t) * (size_t)nn, st));
+  FLG_CUDA(ctx, cudaMemsetAsync(T.lpar, 0xFF, sizeof(int32_t) * (size_t)n, st));
+  const unsigned g = grid_for(nn, 256, (int64_t)ctx->num_sms * 8);
+  k_tl_init<<<g, 256, 0, st>>>(b->d_nodes2, nn, b->d_tri_off, b->n_scenes, T, ctx->d_err);
+  FLG_LAUNCH_CHECK(ctx, "k_tl_init");
+  static const int round_per_sm = [] {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_tl_round, kTlThreads, 0) != cudaSuccess || v < 1) v = 1;
+    return v;
+  }();
+  for (int r = 0; r < kTlRounds; ++r) {
+    k_tl_round<<<grid_for(n, kTlThreads, (int64_t)ctx->num_sms * round_per_sm), kTlThreads, 0, st>>>(
+        n, kTreelet << r, T);
+    FLG_LAUNCH_CHECK(ctx, "k_tl_round");
+  }
+  stage_mark(ctx, st, "treelet");
+  k_tl_first<<<grid_for(nn + n, 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(nn, n, b->d_tri_off, b->n_scenes, T);
+  FLG_LAUNCH_CHECK(ctx, "k_tl_first");
+  k_tl_emit<<<g, 256, 0, st>>>(nn, b->d_tri_off, b->n_scenes, T, b->d_tl_nodes);
+  FLG_LAUNCH_CHECK(ctx, "k_tl_emit");
+  k_tl_leaves<<<grid_for(n, 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(n, T, b->d_perm, b->d_tl_perm,
+                                                                           b->d_tl_tris);
+  FLG_LAUNCH_CHECK(ctx, "k_tl_leaves");
+  FLG_CUDA(ctx, cudaMemcpyAsync(b->d_nodes2, b->d_tl_nodes, sizeof(Node2) * (size_t)nn, cudaMemcpyDeviceToDevice, st));
+  FLG_CUDA(ctx, cudaMemcpyAsync(b->d_perm, b->d_tl_perm, sizeof(uint32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+  FLG_CUDA(ctx, cudaMemcpyAsync(b->d_tris, b->d_tl_tris, sizeof(TriRec) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+  stage_mark(ctx, st, "treelet_emit");
+  return FLG_OK;
+}
+
+}  // namespace flg

@@ -75,8 +75,8 @@ typedef struct flg_build_opts {
   int32_t node_width;     /* traversal layout: 2, 4 or 8 (0 = 4) */
   int32_t leaf_size;      /* wide layouts: max triangles per leaf range (0 = 1) */
   int32_t keep_topology;  /* unused: flg_bvh_download derives the Karras arrays from the nodes */
-  int32_t builder;        /* FLG_BUILDER_LBVH (0, the Karras radix tree), FLG_BUILDER_PLOC or
-                             FLG_BUILDER_SAH */
+  int32_t builder;        /* FLG_BUILDER_LBVH (0, the Karras radix tree), FLG_BUILDER_PLOC,
+                             FLG_BUILDER_SAH or FLG_BUILDER_TREELET */
 } flg_build_opts;
 
 /* Tree builders.  FLG_BUILDER_PLOC is a high-quality alternative to the
@@ -94,8 +94,15 @@ typedef struct flg_build_opts {
  * bucket indices clamped to [0, 15], and leaves of k > 1 triangles stored as
  * balanced binary subtrees.  Nodes are numbered as in the Karras tree, so
  * flg_bvh_download returns its topology (morton is not filled).  One host
- * synchronisation per tree level (not capturable). */
-enum { FLG_BUILDER_LBVH = 0, FLG_BUILDER_PLOC = 1, FLG_BUILDER_SAH = 2 };
+ * synchronisation per tree level (not capturable).
+ * FLG_BUILDER_TREELET is the LBVH refined by treelet restructuring (Karras &
+ * Aila 2013): three bottom-up passes, each rebuilding the 7-leaf treelet
+ * below every node whose subtree holds at least 7, 14, 28 triangles into its
+ * topology of least SAH cost (Ci = 1.2, Ct = 1; subset dynamic
+ * programming); leaves are then renumbered in depth-first order and nodes in
+ * Karras' numbering, so flg_bvh_download returns its topology (morton is not
+ * in the new order).  Capturable. */
+enum { FLG_BUILDER_LBVH = 0, FLG_BUILDER_PLOC = 1, FLG_BUILDER_SAH = 2, FLG_BUILDER_TREELET = 3 };
 
 typedef struct flg_trace_opts {
   int32_t stack_depth;    /* 32 or 64 (0 = 64); overflowing rays are retried deeper */

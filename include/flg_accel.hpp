@@ -265,14 +265,17 @@ class GpuLBVH {
   }
 
   // Primitive::intersect for one ray (one trace launch; prefer the batch).
-  bool intersect(const Ray &ray, SInteraction &isect) {
+  // prim (optional) receives the hit triangle's index, -1 on a miss, so that
+  // a caller can set isect.m_primitive from its own primitive list.
+  bool intersect(const Ray &ray, SInteraction &isect, int32_t *prim = nullptr) {
     bool hit = false;
-    intersect(&ray, &isect, &hit, 1);
+    intersect(&ray, &isect, &hit, 1, prim);
     return hit;
   }
 
-  // Primitive::intersect for n rays: hit[i] as the one-ray call returns it.
-  void intersect(const Ray *rays, SInteraction *isect, bool *hit, int64_t n) {
+  // Primitive::intersect for n rays: hit[i] as the one-ray call returns it;
+  // prim_out (optional, n entries) the hit triangles.
+  void intersect(const Ray *rays, SInteraction *isect, bool *hit, int64_t n, int32_t *prim_out = nullptr) {
     if (n <= 0) return;
     std::vector<float> soa(8 * (size_t)n);
     for (int64_t i = 0; i < n; ++i) {
@@ -301,6 +304,7 @@ class GpuLBVH {
     using V = std::decay_t<decltype(isect[0].m_p)>;
     for (int64_t i = 0; i < n; ++i) {
       hit[i] = prim[i] >= 0;
+      if (prim_out) prim_out[i] = prim[i];
       if (!hit[i]) continue;
       const Ray &ray = rays[i];
       const float th = t[i];

@@ -958,6 +958,237 @@ ORC_API void orc_build_sah(const float *pos, const int32_t *idx, int64_t n, int3
   for (int64_t i = 0; i < n; ++i) perm[i] = S.r[i].orig;
 }
 
+// ---------------------------------------------------------------------------
+// Treelet restructuring of the LBVH (Karras & Aila, "Fast Parallel
+// Construction of High-Quality Bounding Volume Hierarchies", HPG 2013; no
+// counterpart in the reference, whose quality builder is the binned SAH of
+// base_bvh.cpp:33-173).  `rounds` bottom-up passes; pass r visits every
+// internal node after both its children (post order) and, when its subtree
+// holds at least 7 << r triangles, rebuilds the treelet of its 7 largest
+// descendants (repeatedly opening the treelet leaf of largest surface area,
+// first in list order on ties; the opened node's left child takes its place
+// and its right child is appended) into the topology of least SAH cost
+//   C(S) = Ci A(S) + min over splits {P, S \ P} of C(P) + C(S \ P),
+// P holding the lowest member of S, splits enumerated from S - 1 downwards,
+// the first minimum kept; a treelet leaf costs its subtree's SAH cost
+// (a triangle Ct A).  A = dx dy + dy dz + dz dx (half the surface area),
+// Ci = 1.2, Ct = 1.  The treelet's internal nodes are reused in pre-order.
+// Afterwards the leaves are renumbered in depth-first order and the internal
+// nodes take Karras' numbering (root 0, a left child its last position, a
+// right child its first), so the result has the Karras arrays' form: perm,
+// split, leaf flags, range end, parents, node bounds.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr float kTlCi = 1.2f, kTlCt = 1.0f;
+constexpr int kTreelet = 7;
+
+inline float tl_area(const Bound &b) {
+  const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+  return dx * dy + dy * dz + dz * dx;
+}
+inline Bound tl_union(const Bound &a, const Bound &b) {
+  Bound r;
+  for (int k = 0; k < 3; ++k) {
+    r.lo[k] = std::min(a.lo[k], b.lo[k]);
+    r.hi[k] = std::max(a.hi[k], b.hi[k]);
+  }
+  return r;
+}
+
+struct Treelets {
+  int64_t n;
+  // internal nodes 0 .. n-2 (the LBVH's slots); refs >= 0 internal, < 0 ~leaf
+  std::vector<int32_t> left, right, parent, nleaf;  // parent of the root: -1
+  std::vector<int32_t> leaf_par;                    // per leaf (old sorted position)
+  std::vector<Bound> box;
+  std::vector<float> cost;
+  std::vector<Bound> lbox;  // per leaf: triangle box
+  Bound bx(int32_t r) const { return r >= 0 ? box[r] : lbox[~r]; }
+  float cs(int32_t r) const { return r >= 0 ? cost[r] : kTlCt * tl_area(lbox[~r]); }
+  int32_t nl(int32_t r) const { return r >= 0 ? nleaf[r] : 1; }
+  void set_parent(int32_t r, int32_t p) {
+    if (r >= 0) parent[r] = p; else leaf_par[~r] = p;
+  }
+
+  void finish(int32_t x) {  // box, cost and count from the children
+    const int32_t l = left[x], r = right[x];
+    box[x] = tl_union(bx(l), bx(r));
+    cost[x] = kTlCi * tl_area(box[x]) + (cs(l) + cs(r));
+    nleaf[x] = nl(l) + nl(r);
+  }
+
+  void restructure(int32_t R) {
+    int32_t L[kTreelet], I[kTreelet - 1];
+    int nL = 2, nI = 1;
+    L[0] = left[R];
+    L[1] = right[R];
+    I[0] = R;
+    while (nL < kTreelet) {
+      int best = -1;
+      float ba = -1.0f;
+      for (int k = 0; k < nL; ++k)
+        if (L[k] >= 0) {
+          const float a = tl_area(box[L[k]]);
+          if (a > ba) {
+            ba = a;
+            best = k;
+          }
+        }
+      if (best < 0) return;
+      const int32_t x = L[best];
+      I[nI++] = x;
+      L[best] = left[x];
+      L[nL++] = right[x];
+    }
+    constexpr int kFull = (1 << kTreelet) - 1;
+    float c[kFull + 1], a[kFull + 1];
+    int part[kFull + 1];
+    Bound sb[kFull + 1];
+    for (int S = 1; S <= kFull; ++S) {
+      const int low = S & -S;
+      const int li = __builtin_ctz((unsigned)low);
+      sb[S] = S == low ? bx(L[li]) : tl_union(sb[S ^ low], bx(L[li]));
+      a[S] = tl_area(sb[S]);
+      if (S == low) {
+        c[S] = cs(L[li]);
+        part[S] = 0;
+        continue;
+      }
+      float best = FLT_MAX;
+      int bp = 0;
+      for (int P = (S - 1) & S; P > 0; P = (P - 1) & S) {
+        if (!(P & low)) continue;
+        const float v = c[P] + c[S ^ P];
+        if (v < best) {
+          best = v;
+          bp = P;
+        }
+      }
+      c[S] = kTlCi * a[S] + best;
+      part[S] = bp;
+    }
+    // rebuild: internal nodes of the treelet in pre-order, left before right
+    int next = 1;
+    struct Item { int S; int32_t node; };
+    Item st[kTreelet];
+    int sp = 0;
+    st[sp++] = Item{kFull, R};
+    // pre-order assignment, then box / cost / count bottom-up
+    int32_t order[kTreelet - 1];
+    int no = 0;
+    while (sp) {
+      const Item it = st[--sp];
+      order[no++] = it.node;
+      const int P = part[it.S], Q = it.S ^ P;
+      int32_t ch[2];
+      const int sub[2] = {P, Q};
+      for (int k = 0; k < 2; ++k) {
+        if (__builtin_popcount((unsigned)sub[k]) == 1) {
+          ch[k] = L[__builtin_ctz((unsigned)sub[k])];
+        } else {
+          ch[k] = I[next++];
+        }
+      }
+      left[it.node] = ch[0];
+      right[it.node] = ch[1];
+      set_parent(ch[0], it.node);
+      set_parent(ch[1], it.node);
+      // right first on the stack so that the left subtree takes the next nodes
+      if (__builtin_popcount((unsigned)Q) > 1) st[sp++] = Item{Q, ch[1]};
+      if (__builtin_popcount((unsigned)P) > 1) st[sp++] = Item{P, ch[0]};
+    }
+    for (int k = no - 1; k >= 0; --k) finish(order[k]);
+  }
+
+  void pass(int32_t x, int64_t gamma) {  // post order
+    if (left[x] >= 0) pass(left[x], gamma);
+    if (right[x] >= 0) pass(right[x], gamma);
+    finish(x);
+    if (nleaf[x] >= gamma) restructure(x);
+  }
+};
+}  // namespace
+
+ORC_API void orc_build_treelet(const float *pos, const int32_t *idx, int64_t n, int32_t rounds, int32_t *perm,
+                               int32_t *split, uint8_t *leaf, int32_t *range_j, int32_t *parent,
+                               int32_t *leaf_parent, float *nb) {
+  Mesh M{pos, idx, n};
+  // the LBVH (radix_bvh.cpp:32-200)
+  float sb[6];
+  orc_scene_bound(pos, idx, n, sb);
+  std::vector<uint32_t> codes((size_t)n), sc((size_t)n);
+  std::vector<int32_t> p0((size_t)n);
+  orc_morton(pos, idx, n, sb, codes.data());
+  orc_sort(codes.data(), n, sc.data(), p0.data());
+  if (n < 2) {
+    for (int64_t i = 0; i < n; ++i) perm[i] = p0[i];
+    if (n == 1) leaf_parent[0] = -1;
+    return;
+  }
+  std::vector<int32_t> sp((size_t)n - 1), kp((size_t)n - 1), klp((size_t)n), rj((size_t)n - 1);
+  std::vector<uint8_t> lf((size_t)n - 1);
+  orc_karras(sc.data(), n, sp.data(), lf.data(), rj.data(), kp.data(), klp.data());
+  Treelets T;
+  T.n = n;
+  T.left.resize(n - 1);
+  T.right.resize(n - 1);
+  T.parent.resize(n - 1);
+  T.nleaf.resize(n - 1);
+  T.box.resize(n - 1);
+  T.cost.resize(n - 1);
+  T.leaf_par.resize(n);
+  T.lbox.resize(n);
+  for (int64_t i = 0; i < n; ++i) T.lbox[i] = M.bound(p0[i]);
+  for (int64_t i = 0; i + 1 < n; ++i) {
+    T.left[i] = (lf[i] & 1) ? ~sp[i] : sp[i];
+    T.right[i] = (lf[i] & 2) ? ~(sp[i] + 1) : sp[i] + 1;
+  }
+  for (int64_t i = 0; i + 1 < n; ++i) {
+    T.set_parent(T.left[i], (int32_t)i);
+    T.set_parent(T.right[i], (int32_t)i);
+  }
+  T.parent[0] = -1;
+  for (int r = 0; r < rounds; ++r) T.pass(0, (int64_t)kTreelet << r);
+  if (rounds == 0) {  // boxes, costs and counts of the plain LBVH
+    std::vector<int32_t> st{0}, ord;
+    while (!st.empty()) {
+      const int32_t x = st.back();
+      st.pop_back();
+      ord.push_back(x);
+      if (T.left[x] >= 0) st.push_back(T.left[x]);
+      if (T.right[x] >= 0) st.push_back(T.right[x]);
+    }
+    for (size_t k = ord.size(); k-- > 0;) T.finish(ord[k]);
+  }
+  // depth-first renumbering and Karras slots
+  struct Item { int32_t ref; int64_t first; int32_t pslot; int side; };
+  std::vector<Item> st;
+  st.push_back(Item{0, 0, -1, -1});
+  while (!st.empty()) {
+    const Item it = st.back();
+    st.pop_back();
+    if (it.ref < 0) {
+      perm[it.first] = p0[~it.ref];
+      leaf_parent[it.first] = it.pslot;
+      continue;
+    }
+    const int32_t x = it.ref;
+    const int64_t cnt = T.nleaf[x], last = it.first + cnt - 1;
+    const int32_t slot = (int32_t)(it.side < 0 ? 0 : it.side == 0 ? last : it.first);
+    if (it.pslot >= 0) parent[slot] = it.pslot; else parent[slot] = 0;
+    const int64_t nl = T.nl(T.left[x]);
+    split[slot] = (int32_t)(it.first + nl - 1);
+    leaf[slot] = (uint8_t)((T.left[x] < 0 ? 1 : 0) | (T.right[x] < 0 ? 2 : 0));
+    range_j[slot] = (int32_t)(slot == it.first ? last : it.first);
+    for (int k = 0; k < 3; ++k) {
+      nb[6 * (int64_t)slot + k] = T.box[x].lo[k];
+      nb[6 * (int64_t)slot + 3 + k] = T.box[x].hi[k];
+    }
+    st.push_back(Item{T.right[x], it.first + nl, slot, 1});
+    st.push_back(Item{T.left[x], it.first, slot, 0});
+  }
+}
+
 // Closest hit over a tree built by the functions above (recursiveIntersect).
 // rays: 8 SoA arrays of n floats (ox oy oz dx dy dz tmin tmax).  out: prim
 // (-1 = miss), t, u, v.

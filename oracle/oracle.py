@@ -172,6 +172,27 @@ def build_bvh_sah(pos, idx=None, n_tri=None):
     return t
 
 
+def build_bvh_treelet(pos, idx=None, n_tri=None, rounds=3):
+    """The LBVH after `rounds` passes of treelet restructuring (7-leaf
+    treelets, SAH), renumbered in depth-first leaf order, in the Karras
+    arrays' form: perm, split, leaf_flags, range_j, parent, leaf_parent, node
+    bounds and the scene bound."""
+    pos = _f32(pos).reshape(-1, 3)
+    idx = None if idx is None else _i32(idx).reshape(-1, 3)
+    n = idx.shape[0] if idx is not None else pos.shape[0] // 3
+    if n_tri is not None:
+        n = n_tri
+    m = max(n - 1, 0)
+    t = {"perm": np.zeros(n, np.int32), "split": np.zeros(m, np.int32), "leaf_flags": np.zeros(m, np.uint8),
+         "range_j": np.zeros(m, np.int32), "parent": np.zeros(m, np.int32), "leaf_parent": np.zeros(n, np.int32),
+         "bounds": np.zeros((m, 6), np.float32)}
+    lib().orc_build_treelet(_p(pos), _p(idx), C.c_int64(n), C.c_int32(rounds), _p(t["perm"]), _p(t["split"]),
+                            _p(t["leaf_flags"]), _p(t["range_j"]), _p(t["parent"]), _p(t["leaf_parent"]),
+                            _p(t["bounds"]))
+    t.update({"scene_bound": scene_bound(pos, idx, n), "n": n})
+    return t
+
+
 def build_timed(pos, idx, n):
     """Reference-performance build (parallel, 32-byte records); returns arrays."""
     pos, idx = _f32(pos), _i32(idx)

@@ -87,9 +87,10 @@ def test_builder_ids_match_header():
     import fledge_gb300._lib as L
     text = open(HEADER).read()
     enum = dict(re.findall(r"(FLG_BUILDER_\w+)\s*=\s*(\d+)", text))
-    assert enum == {"FLG_BUILDER_LBVH": "0", "FLG_BUILDER_PLOC": "1", "FLG_BUILDER_SAH": "2"}
+    assert enum == {"FLG_BUILDER_LBVH": "0", "FLG_BUILDER_PLOC": "1", "FLG_BUILDER_SAH": "2",
+                    "FLG_BUILDER_TREELET": "3"}
     for k, v in enum.items():
         assert getattr(L, k) == int(v)
-    assert [F._builder_id(n) for n in ("lbvh", "ploc", "sah")] == [0, 1, 2]
+    assert [F._builder_id(n) for n in ("lbvh", "ploc", "sah", "treelet")] == [0, 1, 2, 3]
     with pytest.raises(ValueError):
         F._builder_id("median")
