@@ -507,19 +507,27 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             hb.intersect_batched(rays, roffs, out=hits, **topts)  # warm-up
             torch.cuda.synchronize()
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            ctx.set_stage_timing(True)
             ev[0].record(stream)
             hb.build()
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            bst = ctx.stage_times()
+            ctx.set_stage_timing(False)
+            hb_ms = ev[0].elapsed_time(ev[1])
+            ctx.sync()
             ev[1].record(stream)
             hb.intersect_batched(rays, roffs, out=hits, **topts)
             ev[2].record(stream)
             torch.cuda.synchronize()
-            hb_ms, ht_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+            ht_ms = ev[1].elapsed_time(ev[2])
             res[name] = {"builder": {"ploc": "ploc (radius 16)", "sah": "binned SAH (16 buckets, reference rule)",
                                      "treelet": "LBVH + 3 rounds of 7-leaf treelet restructuring"}[name],
                          "build_ms": round(hb_ms, 3), "trace_ms": round(ht_ms, 2),
                          "mrays_s": round(n_rays / (ht_ms * 1e-3) / 1e6, 1),
                          "trace_speedup_vs_lbvh": round(statistics.median(trace_ms) / ht_ms, 3),
-                         "step_ms": round(hb_ms + ht_ms, 2)}
+                         "step_ms": round(hb_ms + ht_ms, 2),
+                         "build_stages_ms": {k: round(v["ms"], 3) for k, v in bst.items()}}
             hb.destroy()
             log(f'{name} builder done')
         hq, sah, tl = res["ploc"], res["sah"], res["treelet"]

@@ -30,7 +30,7 @@ namespace flg {
 constexpr float kTlCi = 1.2f, kTlCt = 1.0f;
 constexpr int kTreelet = 7, kTlFull = (1 << kTreelet) - 1;
 constexpr int kTlRounds = 3;
-constexpr int kTlThreads = 64;
+constexpr int kTlThreads = 128;
 
 struct TlBox {
   float lo[3], hi[3];
@@ -46,6 +46,54 @@ __device__ __forceinline__ void tl_merge(TlBox &a, const TlBox &b) {
     a.hi[k] = fmaxf(a.hi[k], b.hi[k]);
   }
 }
+
+// Subsets of the 7 treelet leaves ordered by size: kTlCount[k] subsets of
+// size k from kTlOffset[k].
+__constant__ uint8_t kTlSubsets[kTlFull] = {
+    1,   2,   4,   8,   16,  32,  64,  3,   5,   6,   9,   10,  12,  17,  18,  20,  24,  33,  34,  36,  40,  48,
+    65,  66,  68,  72,  80,  96,  7,   11,  13,  14,  19,  21,  22,  25,  26,  28,  35,  37,  38,  41,  42,  44,
+    49,  50,  52,  56,  67,  69,  70,  73,  74,  76,  81,  82,  84,  88,  97,  98,  100, 104, 112, 15,  23,  27,
+    29,  30,  39,  43,  45,  46,  51,  53,  54,  57,  58,  60,  71,  75,  77,  78,  83,  85,  86,  89,  90,  92,
+    99,  101, 102, 105, 106, 108, 113, 114, 116, 120, 31,  47,  55,  59,  61,  62,  79,  87,  91,  93,  94,  103,
+    107, 109, 110, 115, 117, 118, 121, 122, 124, 63,  95,  111, 119, 123, 125, 126, 127};
+__constant__ int kTlCount[kTreelet + 1] = {0, 7, 21, 35, 35, 21, 7, 1};
+__constant__ int kTlOffset[kTreelet + 1] = {0, 0, 7, 28, 63, 98, 119, 126};
+
+// The bits of t deposited, lowest first, at the set bits of mask.
+__device__ __forceinline__ int tl_deposit(int t, int mask) {
+  int q = 0;
+  for (; mask; mask &= mask - 1, t >>= 1)
+    if (t & 1) q |= mask & -mask;
+  return q;
+}
+
+// One warp's treelet in shared memory: the leaves' boxes, costs and counts,
+// every subset's area, least cost and split, the grown L / I lists and the
+// rebuilt internal nodes.
+struct TlWarp {
+  float lo[kTreelet][3], hi[kTreelet][3];
+  float c[kTlFull + 1], area[kTlFull + 1];
+  int32_t ln[kTreelet], L[kTreelet], I[kTreelet - 1], order[kTreelet - 1];
+  int orderS[kTreelet - 1];
+  uint8_t part[kTlFull + 1];
+
+  // union of the leaves of S: the lowest first, then every member in order
+  __device__ __forceinline__ TlBox uni(int S) const {
+    const int f = __ffs(S) - 1;
+    TlBox u;
+    for (int q = 0; q < 3; ++q) {
+      u.lo[q] = lo[f][q];
+      u.hi[q] = hi[f][q];
+    }
+    for (int k = 0; k < kTreelet; ++k)
+      if ((S >> k) & 1)
+        for (int q = 0; q < 3; ++q) {
+          u.lo[q] = fminf(u.lo[q], lo[k][q]);
+          u.hi[q] = fmaxf(u.hi[q], hi[k][q]);
+        }
+    return u;
+  }
+};
 
 // Working form: per node slot children (>= 0 node slot, < 0 ~sorted leaf),
 // parent (-1 at a root), leaf count, SAH cost, box; per leaf its parent.
@@ -93,111 +141,158 @@ struct Tl {
     nleaf[x] = n;
   }
 
-  __device__ void finish(int32_t x) const {
+  __device__ int32_t finish(int32_t x) const {
     const int32_t l = __ldcg(left + x), r = __ldcg(right + x);
     TlBox b = bx(l);
     tl_merge(b, bx(r));
-    store(x, b, kTlCi * tl_area(b) + (cs(l) + cs(r)), nl(l) + nl(r));
+    const int32_t n = nl(l) + nl(r);
+    store(x, b, kTlCi * tl_area(b) + (cs(l) + cs(r)), n);
+    return n;
   }
 
-  __device__ void restructure(int32_t R) const {
-    int32_t L[kTreelet], I[kTreelet - 1];
-    int nL = 2, nI = 1;
-    L[0] = __ldcg(left + R);
-    L[1] = __ldcg(right + R);
-    I[0] = R;
-    while (nL < kTreelet) {
-      int best = -1;
-      float ba = -1.0f;
-      for (int k = 0; k < nL; ++k)
-        if (L[k] >= 0) {
-          const float a = tl_area(bx(L[k]));
-          if (a > ba) {
-            ba = a;
-            best = k;
+  // Rebuilds the treelet rooted at R with the whole warp (R uniform, every
+  // lane calls).  Decisions equal the serial rule: the growing picks the
+  // first treelet leaf of largest area, a subset's split is the first
+  // minimum in the order P = (S - 1) & S downwards; lanes split the
+  // candidates and reduce (cost, position in that order).
+  __device__ void restructure(int32_t R, TlWarp &w, int lane) const {
+    if (lane == 0) {
+      w.L[0] = __ldcg(left + R);
+      w.L[1] = __ldcg(right + R);
+      w.I[0] = R;
+    }
+    __syncwarp();
+    for (int nL = 2; nL < kTreelet; ++nL) {
+      const int32_t mine = lane < nL ? w.L[lane] : -1;
+      float a = -2.0f;
+      int k = 32;
+      if (mine >= 0) {
+        const float v = tl_area(bx(mine));
+        if (v > -1.0f) {
+          a = v;
+          k = lane;
+        }
+      }
+      for (int o = 4; o; o >>= 1) {
+        const float oa = __shfl_xor_sync(0xffffffffu, a, o);
+        const int ok = __shfl_xor_sync(0xffffffffu, k, o);
+        if (oa > a || (oa == a && ok < k)) {
+          a = oa;
+          k = ok;
+        }
+      }
+      k = __shfl_sync(0xffffffffu, k, 0);
+      if (k == 32) return;  // every treelet leaf is a triangle
+      __syncwarp();
+      if (lane == 0) {
+        const int32_t x = w.L[k];
+        w.I[nL - 1] = x;
+        w.L[k] = __ldcg(left + x);
+        w.L[nL] = __ldcg(right + x);
+      }
+      __syncwarp();
+    }
+    if (lane < kTreelet) {
+      const int32_t r = w.L[lane];
+      const TlBox b = bx(r);
+      for (int q = 0; q < 3; ++q) {
+        w.lo[lane][q] = b.lo[q];
+        w.hi[lane][q] = b.hi[q];
+      }
+      w.c[1 << lane] = cs(r);
+      w.part[1 << lane] = 0;
+      w.ln[lane] = nl(r);
+    }
+    __syncwarp();
+    for (int S = lane + 1; S <= kTlFull; S += 32) w.area[S] = tl_area(w.uni(S));
+    __syncwarp();
+    // sizes 2..7: 21, 35, 35, 21, 7, 1 subsets; 1, 1, 1, 1, 4, 32 lanes each
+    for (int k = 2; k <= kTreelet; ++k) {
+      const int m = kTlCount[k], g = k == 7 ? 32 : k == 6 ? 4 : 1, np = (1 << (k - 1)) - 1;
+      for (int base = 0; base < m; base += 32 / g) {
+        const int si = base + lane / g, r = lane % g;
+        const bool ok = si < m;
+        const int S = ok ? (int)kTlSubsets[kTlOffset[k] + si] : 0;
+        const int low = S & -S, rest = S ^ low;
+        float best = 3.402823466e+38f;
+        int bj = np, bp = 0;
+        if (ok) {
+          // The j-th split holding `low` is low | Q, Q the (np - 1 - j)-th
+          // subset of rest; Q = (Q - 1) & rest steps to the next j.
+          int Q = tl_deposit(np - 1 - r, rest);
+          for (int j = r; j < np; j += g) {
+            const int P = low | Q;
+            const float v = w.c[P] + w.c[S ^ P];
+            if (v < best) {
+              best = v;
+              bj = j;
+              bp = P;
+            }
+            if (g == 32) {
+              Q = tl_deposit(np - 1 - (j + g), rest);
+            } else {
+              for (int q = 0; q < g; ++q) Q = (Q - 1) & rest;
+            }
           }
         }
-      if (best < 0) return;
-      const int32_t x = L[best];
-      I[nI++] = x;
-      L[best] = __ldcg(left + x);
-      L[nL++] = __ldcg(right + x);
-    }
-    TlBox lb[kTreelet];
-    float lc[kTreelet];
-    int32_t ln[kTreelet];
-    for (int k = 0; k < kTreelet; ++k) {
-      lb[k] = bx(L[k]);
-      lc[k] = cs(L[k]);
-      ln[k] = nl(L[k]);
-    }
-    float c[kTlFull + 1];
-    uint8_t part[kTlFull + 1];
-    for (int S = 1; S <= kTlFull; ++S) {
-      const int low = S & -S;
-      if (S == low) {
-        c[S] = lc[__ffs(low) - 1];
-        part[S] = 0;
-        continue;
-      }
-      TlBox u = lb[__ffs(low) - 1];
-      for (int k = 0; k < kTreelet; ++k)
-        if ((S >> k) & 1) tl_merge(u, lb[k]);
-      float best = 3.402823466e+38f;
-      int bp = 0;
-      for (int P = (S - 1) & S; P > 0; P = (P - 1) & S) {
-        if (!(P & low)) continue;
-        const float v = c[P] + c[S ^ P];
-        if (v < best) {
-          best = v;
-          bp = P;
+        for (int o = g >> 1; o; o >>= 1) {
+          const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+          const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+          const int op = __shfl_xor_sync(0xffffffffu, bp, o);
+          if (ob < best || (ob == best && oj < bj)) {
+            best = ob;
+            bj = oj;
+            bp = op;
+          }
+        }
+        if (ok && r == 0) {
+          w.c[S] = kTlCi * w.area[S] + best;
+          w.part[S] = (uint8_t)bp;
         }
       }
-      c[S] = kTlCi * tl_area(u) + best;
-      part[S] = (uint8_t)bp;
+      __syncwarp();
     }
     // Rebuild: internal nodes taken from I as their parents are expanded
     // (left child first), expansion by a stack with the left subtree on top.
-    int next = 1, sp = 0, no = 0;
-    int stS[kTreelet];
-    int32_t stN[kTreelet], order[kTreelet - 1];
-    int orderS[kTreelet - 1];
-    stS[sp] = kTlFull;
-    stN[sp++] = R;
-    while (sp) {
-      --sp;
-      const int S = stS[sp];
-      const int32_t node = stN[sp];
-      order[no] = node;
-      orderS[no++] = S;
-      const int P = part[S], Q = S ^ P;
-      const int32_t c0 = __popc(P) == 1 ? L[__ffs(P) - 1] : I[next++];
-      const int32_t c1 = __popc(Q) == 1 ? L[__ffs(Q) - 1] : I[next++];
-      left[node] = c0;
-      right[node] = c1;
-      set_parent(c0, node);
-      set_parent(c1, node);
-      if (__popc(Q) > 1) {
-        stS[sp] = Q;
-        stN[sp++] = c1;
-      }
-      if (__popc(P) > 1) {
-        stS[sp] = P;
-        stN[sp++] = c0;
+    if (lane == 0) {
+      int next = 1, sp = 0, no = 0;
+      int stS[kTreelet];
+      int32_t stN[kTreelet];
+      stS[sp] = kTlFull;
+      stN[sp++] = R;
+      while (sp) {
+        --sp;
+        const int S = stS[sp];
+        const int32_t node = stN[sp];
+        w.order[no] = node;
+        w.orderS[no++] = S;
+        const int P = w.part[S], Q = S ^ P;
+        const int32_t c0 = __popc(P) == 1 ? w.L[__ffs(P) - 1] : w.I[next++];
+        const int32_t c1 = __popc(Q) == 1 ? w.L[__ffs(Q) - 1] : w.I[next++];
+        left[node] = c0;
+        right[node] = c1;
+        set_parent(c0, node);
+        set_parent(c1, node);
+        if (__popc(Q) > 1) {
+          stS[sp] = Q;
+          stN[sp++] = c1;
+        }
+        if (__popc(P) > 1) {
+          stS[sp] = P;
+          stN[sp++] = c0;
+        }
       }
     }
-    // boxes, counts and costs bottom-up (children were expanded later)
-    for (int k = no - 1; k >= 0; --k) {
-      const int S = orderS[k];
-      TlBox u = lb[__ffs(S & -S) - 1];
+    __syncwarp();
+    // boxes, counts and costs of the treelet's six internal nodes
+    if (lane < kTreelet - 1) {
+      const int S = w.orderS[lane];
       int32_t n = 0;
       for (int j = 0; j < kTreelet; ++j)
-        if ((S >> j) & 1) {
-          tl_merge(u, lb[j]);
-          n += ln[j];
-        }
-      store(order[k], u, c[S], n);
+        if ((S >> j) & 1) n += w.ln[j];
+      store(w.order[lane], w.uni(S), w.c[S], n);
     }
+    __syncwarp();
   }
 };
 
@@ -231,23 +326,36 @@ __global__ void __launch_bounds__(256)
 }
 
 // One round: a thread per leaf climbs; the second arrival at a node finishes
-// it (and rebuilds its treelet when its subtree is large enough).
+// it.  Nodes whose subtree is large enough are then rebuilt by the whole
+// warp, one after the other: the nodes that one warp finishes in one step
+// lie in disjoint subtrees (a node is finished only after its whole
+// subtree), so their order does not matter.
 __global__ void __launch_bounds__(kTlThreads)
     k_tl_round(int64_t n_tri, int32_t gamma, Tl T) {
-  for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n_tri;
-       pos += (int64_t)gridDim.x * blockDim.x) {
-    int32_t x = __ldcg(T.lpar + pos);
+  __shared__ TlWarp warps[kTlThreads / 32];
+  TlWarp &w = warps[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n_tri;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    int32_t x = base + lane < n_tri ? __ldcg(T.lpar + base + lane) : -1;
     // a valid tree is at most 62 levels deep; the bound only matters for a
     // tree left inconsistent by an earlier timed-out build
-    for (int depth = 0; x >= 0 && depth < 128; ++depth) {
+    for (int depth = 0; __any_sync(0xffffffffu, x >= 0); ++depth) {
+      bool big = false;
+      if (x >= 0) {
+        __threadfence();
+        if (atomicAdd(T.flag + x, 1u) == 0u) {
+          x = -1;
+        } else {
+          T.flag[x] = 0u;  // both arrivals seen: ready for the next round
+          __threadfence();
+          big = T.finish(x) >= gamma;
+        }
+      }
+      for (unsigned need = __ballot_sync(0xffffffffu, big); need; need &= need - 1)
+        T.restructure(__shfl_sync(0xffffffffu, x, __ffs(need) - 1), w, lane);
       __threadfence();
-      if (atomicAdd(T.flag + x, 1u) == 0u) break;
-      T.flag[x] = 0u;  // both arrivals seen: ready for the next round
-      __threadfence();
-      T.finish(x);
-      if (__ldcg(T.nleaf + x) >= gamma) T.restructure(x);
-      __threadfence();
-      x = __ldcg(T.parent + x);
+      if (x >= 0) x = depth < 127 ? __ldcg(T.parent + x) : -1;
     }
   }
 }
@@ -378,6 +486,7 @@ int treelet_build(flg_ctx ctx, flg_bvh b) {
   stage_mark(ctx, st, "treelet");
   k_tl_first<<<grid_for(nn + n, 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(nn, n, b->d_tri_off, b->n_scenes, T);
   FLG_LAUNCH_CHECK(ctx, "k_tl_first");
+  stage_mark(ctx, st, "treelet_first");
   k_tl_emit<<<g, 256, 0, st>>>(nn, b->d_tri_off, b->n_scenes, T, b->d_tl_nodes);
   FLG_LAUNCH_CHECK(ctx, "k_tl_emit");
   k_tl_leaves<<<grid_for(n, 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(n, T, b->d_perm, b->d_tl_perm,

@@ -39,7 +39,7 @@ def test_treelet_soup_matches_oracle(ctx, oracle, n):
     _same(b.topology(), oracle.build_bvh_treelet(pos))
 
 
-@pytest.mark.parametrize("case", ["sphere", "clusters", "duplicates"])
+@pytest.mark.parametrize("case", ["sphere", "clusters", "duplicates", "lattice"])
 def test_treelet_special_inputs_match_oracle(ctx, oracle, case):
     rng = np.random.default_rng(7)
     ind = None
@@ -47,6 +47,12 @@ def test_treelet_special_inputs_match_oracle(ctx, oracle, case):
         pos, ind = G.meshed_sphere(120, 120, 1.0)
     elif case == "clusters":
         pos = G.geometric_clusters(40, 60, rng)
+    elif case == "lattice":
+        # equal triangles on an integer lattice: many splits of a treelet
+        # cost exactly the same, so the first-minimum rule decides
+        g = np.stack(np.meshgrid(*[np.arange(20, dtype=np.float32)] * 3, indexing="ij"), -1).reshape(-1, 1, 3)
+        tri = np.array([[0, 0, 0], [0.5, 0, 0], [0, 0.5, 0.25]], np.float32)
+        pos = (g + tri).reshape(-1, 3)
     else:
         pos = np.concatenate([np.tile(G.random_soup(1, rng), (3000, 1)), G.random_soup(500, rng)])
     b, _ = _build(ctx, pos, ind)
