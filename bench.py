@@ -646,10 +646,11 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
     bb.build()
     main = torch.cuda.current_stream(dev)
     copy = torch.cuda.Stream(dev)
-    # scene groups of about 256 M rays
+    # scene groups of about 64 M rays: the first trace waits for one group's
+    # upload and the last download follows the last trace
     groups, g0 = [], 0
     for s in range(N_SCENES):
-        if roffs[s + 1] - roffs[g0] >= (1 << 28) or s == N_SCENES - 1:
+        if roffs[s + 1] - roffs[g0] >= (1 << 26) or s == N_SCENES - 1:
             groups.append((g0, s + 1))
             g0 = s + 1
 
@@ -660,7 +661,10 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
         for (a, b) in groups:
             r0, r1 = int(roffs[a]), int(roffs[b])
             with torch.cuda.stream(copy):
-                d_rays[:, r0:r1].copy_(h_rays[:, r0:r1], non_blocking=True)
+                # one contiguous copy per ray column: a strided [6, m] slice
+                # would go through a pageable host temporary (~50 GB/s)
+                for k in range(6):
+                    d_rays[k, r0:r1].copy_(h_rays[k, r0:r1], non_blocking=True)
                 ev = torch.cuda.Event()
                 ev.record(copy)
             main.wait_event(ev)
