@@ -290,9 +290,12 @@ __device__ __forceinline__ dfl df_div(dfl x, dfl y) {
   return fast_two_sum(q1, q2);
 }
 
-// Hit values of the selected triangle recomputed in float-float with the
-// same Pluecker quantities (t = (v0.N)/(N.D), N = e0 x e1; u = U/S, v = V/S
-// with S = U+V+W = 2 N.D) and rounded once to fp32.  The fp32 test decides
+// Hit values of the selected triangle recomputed in float-float and rounded
+// once to fp32: t = (v0.N)/(N.D) with N = e0 x e1, and the barycentrics of
+// the Pluecker test, u = U/S and v = V/S with S = U+V+W = 2 N.D, through
+// the identities U = 2 e0.(v0 x D) and V = 2 e1.(v0 x D) (the vertex sums of
+// U and V are 2 v0 + e0 and 2 v0 - e1), so u = e0.w / N.D and v = e1.w / N.D
+// with one float-float cross product w = v0 x D.  The fp32 test decides
 // hit/miss and which triangle is closest; this makes the reported t, u, v
 // accurate to about an ulp even for grazing rays, where the fp32 quotients
 // lose digits.  Edges are formed exactly (e0 = c - a, e1 = a - b as
@@ -303,17 +306,10 @@ __device__ __forceinline__ bool refine_tuv(float3 a, float3 b, float3 c, float3 
   const dfl e0x = two_sum(c.x, -a.x), e0y = two_sum(c.y, -a.y), e0z = two_sum(c.z, -a.z);
   const dfl e1x = two_sum(a.x, -b.x), e1y = two_sum(a.y, -b.y), e1z = two_sum(a.z, -b.z);
   const dfl v0x = two_sum(a.x, -O.x), v0y = two_sum(a.y, -O.y), v0z = two_sum(a.z, -O.z);
-  const dfl v1x = two_sum(b.x, -O.x), v1y = two_sum(b.y, -O.y), v1z = two_sum(b.z, -O.z);
-  const dfl v2x = two_sum(c.x, -O.x), v2y = two_sum(c.y, -O.y), v2z = two_sum(c.z, -O.z);
-  const dfl s0x = df_add(v2x, v0x), s0y = df_add(v2y, v0y), s0z = df_add(v2z, v0z);
-  const dfl s1x = df_add(v0x, v1x), s1y = df_add(v0y, v1y), s1z = df_add(v0z, v1z);
-  // U = (e0 x s0) . D, V = (e1 x s1) . D
-  const dfl U = df_add(df_add(df_mulf(df_sub(df_mul(e0y, s0z), df_mul(e0z, s0y)), D.x),
-                              df_mulf(df_sub(df_mul(e0z, s0x), df_mul(e0x, s0z)), D.y)),
-                       df_mulf(df_sub(df_mul(e0x, s0y), df_mul(e0y, s0x)), D.z));
-  const dfl V = df_add(df_add(df_mulf(df_sub(df_mul(e1y, s1z), df_mul(e1z, s1y)), D.x),
-                              df_mulf(df_sub(df_mul(e1z, s1x), df_mul(e1x, s1z)), D.y)),
-                       df_mulf(df_sub(df_mul(e1x, s1y), df_mul(e1y, s1x)), D.z));
+  // w = v0 x D
+  const dfl wx = df_sub(df_mulf(v0y, D.z), df_mulf(v0z, D.y));
+  const dfl wy = df_sub(df_mulf(v0z, D.x), df_mulf(v0x, D.z));
+  const dfl wz = df_sub(df_mulf(v0x, D.y), df_mulf(v0y, D.x));
   // N = e0 x e1
   const dfl Nx = df_sub(df_mul(e0y, e1z), df_mul(e0z, e1y));
   const dfl Ny = df_sub(df_mul(e0z, e1x), df_mul(e0x, e1z));
@@ -321,8 +317,9 @@ __device__ __forceinline__ bool refine_tuv(float3 a, float3 b, float3 c, float3 
   const dfl den = df_add(df_add(df_mulf(Nx, D.x), df_mulf(Ny, D.y)), df_mulf(Nz, D.z));
   if (den.hi == 0.0f) return false;
   const dfl num = df_add(df_add(df_mul(v0x, Nx), df_mul(v0y, Ny)), df_mul(v0z, Nz));
-  const dfl S = dfl{2.0f * den.hi, 2.0f * den.lo};
-  const dfl tt = df_div(num, den), uu = df_div(U, S), vv = df_div(V, S);
+  const dfl U = df_add(df_add(df_mul(e0x, wx), df_mul(e0y, wy)), df_mul(e0z, wz));
+  const dfl V = df_add(df_add(df_mul(e1x, wx), df_mul(e1y, wy)), df_mul(e1z, wz));
+  const dfl tt = df_div(num, den), uu = df_div(U, den), vv = df_div(V, den);
   t = tt.hi + tt.lo;
   u = uu.hi + uu.lo;
   v = vv.hi + vv.lo;

@@ -373,36 +373,30 @@ inline Dfl df_div(Dfl x, Dfl y) {
 }
 
 // Reported hit values of the GPU path: the selected triangle's Pluecker t,
-// u, v recomputed in float-float (t = (v0.N)/(N.D), N = e0 x e1, u = U/S,
-// v = V/S, S = 2 N.D) and rounded once.
+// u, v recomputed in float-float and rounded once: t = (v0.N)/(N.D),
+// N = e0 x e1; u = U/S, v = V/S, S = 2 N.D, through U = 2 e0.(v0 x D) and
+// V = 2 e1.(v0 x D), i.e. u = e0.w / N.D, v = e1.w / N.D, w = v0 x D.
 inline void refine_tuv(const float *a, const float *b, const float *c, const float *O, const float *D, float &t,
                        float &u, float &v) {
-  Dfl e0[3], e1[3], v0[3], v1[3], v2[3], s0[3], s1[3];
+  Dfl e0[3], e1[3], v0[3], w[3], N[3];
   for (int k = 0; k < 3; ++k) {
     e0[k] = two_sum(c[k], -a[k]);
     e1[k] = two_sum(a[k], -b[k]);
     v0[k] = two_sum(a[k], -O[k]);
-    v1[k] = two_sum(b[k], -O[k]);
-    v2[k] = two_sum(c[k], -O[k]);
   }
-  for (int k = 0; k < 3; ++k) {
-    s0[k] = df_add(v2[k], v0[k]);
-    s1[k] = df_add(v0[k], v1[k]);
-  }
-  auto crossdot = [&](const Dfl *e, const Dfl *s) {
-    return df_add(df_add(df_mulf(df_sub(df_mul(e[1], s[2]), df_mul(e[2], s[1])), D[0]),
-                         df_mulf(df_sub(df_mul(e[2], s[0]), df_mul(e[0], s[2])), D[1])),
-                  df_mulf(df_sub(df_mul(e[0], s[1]), df_mul(e[1], s[0])), D[2]));
-  };
-  Dfl U = crossdot(e0, s0), V = crossdot(e1, s1);
-  Dfl N[3] = {df_sub(df_mul(e0[1], e1[2]), df_mul(e0[2], e1[1])),
-              df_sub(df_mul(e0[2], e1[0]), df_mul(e0[0], e1[2])),
-              df_sub(df_mul(e0[0], e1[1]), df_mul(e0[1], e1[0]))};
+  w[0] = df_sub(df_mulf(v0[1], D[2]), df_mulf(v0[2], D[1]));
+  w[1] = df_sub(df_mulf(v0[2], D[0]), df_mulf(v0[0], D[2]));
+  w[2] = df_sub(df_mulf(v0[0], D[1]), df_mulf(v0[1], D[0]));
+  N[0] = df_sub(df_mul(e0[1], e1[2]), df_mul(e0[2], e1[1]));
+  N[1] = df_sub(df_mul(e0[2], e1[0]), df_mul(e0[0], e1[2]));
+  N[2] = df_sub(df_mul(e0[0], e1[1]), df_mul(e0[1], e1[0]));
   Dfl den = df_add(df_add(df_mulf(N[0], D[0]), df_mulf(N[1], D[1])), df_mulf(N[2], D[2]));
   if (den.hi == 0.0f) return;
-  Dfl num = df_add(df_add(df_mul(v0[0], N[0]), df_mul(v0[1], N[1])), df_mul(v0[2], N[2]));
-  Dfl S = {2.0f * den.hi, 2.0f * den.lo};
-  Dfl tt = df_div(num, den), uu = df_div(U, S), vv = df_div(V, S);
+  auto dot = [](const Dfl *x, const Dfl *y) {
+    return df_add(df_add(df_mul(x[0], y[0]), df_mul(x[1], y[1])), df_mul(x[2], y[2]));
+  };
+  Dfl num = dot(v0, N), U = dot(e0, w), V = dot(e1, w);
+  Dfl tt = df_div(num, den), uu = df_div(U, den), vv = df_div(V, den);
   t = tt.hi + tt.lo;
   u = uu.hi + uu.lo;
   v = vv.hi + vv.lo;
