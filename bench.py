@@ -654,20 +654,31 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
             groups.append((g0, s + 1))
             g0 = s + 1
 
+    # One copy stream carries every copy in order (triangles, all ray groups,
+    # then each group's hits once its trace is done): on this system a
+    # host-to-device and a device-to-host copy running at once each drop to
+    # ~60 GB/s, against ~200 GB/s alone.
     def e2e_step():
-        d_pos.copy_(h_pos, non_blocking=True)
+        with torch.cuda.stream(copy):
+            d_pos.copy_(h_pos, non_blocking=True)
+            pos_ev = torch.cuda.Event()
+            pos_ev.record(copy)
+        main.wait_event(pos_ev)
         bb.build()
-        evs = []
-        for (a, b) in groups:
-            r0, r1 = int(roffs[a]), int(roffs[b])
-            with torch.cuda.stream(copy):
+        up = []
+        with torch.cuda.stream(copy):
+            for (a, b) in groups:
+                r0, r1 = int(roffs[a]), int(roffs[b])
                 # one contiguous copy per ray column: a strided [6, m] slice
-                # would go through a pageable host temporary (~50 GB/s)
+                # would go through a pageable host temporary (~55 GB/s)
                 for k in range(6):
                     d_rays[k, r0:r1].copy_(h_rays[k, r0:r1], non_blocking=True)
                 ev = torch.cuda.Event()
                 ev.record(copy)
-            main.wait_event(ev)
+                up.append(ev)
+        for gi, (a, b) in enumerate(groups):
+            r0, r1 = int(roffs[a]), int(roffs[b])
+            main.wait_event(up[gi])
             ro = np.zeros(N_SCENES + 1, np.int64)
             ro[a + 1:b + 1] = roffs[a + 1:b + 1] - roffs[a]
             ro[b + 1:] = ro[b]
@@ -676,8 +687,6 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
             bb.intersect_batched(sub_rays, ro, out=sub_out, **topts)
             done = torch.cuda.Event()
             done.record(main)
-            evs.append((done, r0, r1))
-        for done, r0, r1 in evs:
             copy.wait_event(done)
             with torch.cuda.stream(copy):
                 for k in h_out:

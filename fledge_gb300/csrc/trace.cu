@@ -1041,7 +1041,11 @@ FLG_API int flg_trace_closest_batched(flg_ctx ctx, flg_bvh bvh, const flg_rays *
       FLG_CUDA(ctx, cudaMalloc((void **)&ctx->d_ray_off, sizeof(int64_t) * (ns + 1)));
       ctx->ray_off_cap = ns + 1;
     }
-    FLG_CUDA(ctx, cudaMemcpy(ctx->d_ray_off, ray_offsets_host, sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice));
+    // Stream-ordered: earlier traces on this stream read the old offsets
+    // first.  From pageable memory the source is staged before the call
+    // returns, and the host does not wait for the stream's earlier work.
+    FLG_CUDA(ctx, cudaMemcpyAsync(ctx->d_ray_off, ray_offsets_host, sizeof(int64_t) * (ns + 1),
+                                  cudaMemcpyHostToDevice, ctx->stream));
     cached.assign(ray_offsets_host, ray_offsets_host + ns + 1);
   }
   return trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, opts, ctx->d_ray_off, ns, out, nullptr);

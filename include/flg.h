@@ -230,9 +230,9 @@ FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *ray
                                    int64_t n, const flg_trace_opts *opts, flg_hits *out_host);
 
 /* Closest hit that allocates nothing (no counterpart in the reference).  For
- * callers that cannot call cudaMalloc when they trace — inside a CUDA stream
- * capture, under an arena that hands out all device memory up front, or in a
- * frame loop where an allocation would synchronise the device — whereas
+ * callers that cannot call cudaMalloc when they trace — under an arena that
+ * hands out all device memory up front, or in a frame loop where an
+ * allocation would synchronise the device — whereas
  * flg_trace_closest allocates its scratch on a context's first trace.  Same
  * kernels and results as flg_trace_closest with default options; the
  * scratch is a fixed 8 MB device array inside the library, held on every GPU

@@ -1,6 +1,6 @@
 """flg_trace_closest_noalloc: closest hit for callers that cannot call
-cudaMalloc when they trace (inside a CUDA stream capture, under an arena that
-owns all device memory, in a frame loop where an allocation would stall).
+cudaMalloc when they trace (under an arena that owns all device memory, in a
+frame loop where an allocation would stall the device).
 Its traversal scratch is a fixed device array inside the library instead of
 the context's lazily allocated buffers.
 
@@ -8,9 +8,8 @@ Checked through the C ABI against flg_trace_closest (same kernels, so the
 bar is bit equality, as for the other traversal layouts), on two calls in a
 row: the second call reuses the shared array the first one left behind, also
 after a call whose rays overflow the short stack into the array's overflow
-list.  A trace captured into a CUDA graph and replayed is checked the same
-way; a first call inside a capture is refused.  Kept in its own file,
-collected last."""
+list.  A first call on a device made inside a stream capture is refused.
+Kept in its own file, collected last."""
 import ctypes as C
 
 import numpy as np
@@ -106,49 +105,6 @@ def test_noalloc_deep_stack_scene_then_plain_scene(ctx, width):
     ctx.sync()
     for k in ("prim", "t", "u", "v"):
         assert np.array_equal(got2[k].cpu().numpy(), ref2[k].cpu().numpy()), k
-
-
-def test_noalloc_captured_in_a_graph_and_replayed(ctx):
-    """The case the entry point exists for: after one call outside a capture
-    (which looks up the scratch), a trace recorded inside flg_graph_begin /
-    flg_graph_end and replayed after the rays change in place gives the hits
-    of flg_trace_closest."""
-    import torch
-    pos = F.gen_triangles(ctx, 80000, 0x5EED)
-    b = F.RadixBVHBuilder(F.InternalTriangleMesh(pos), ctx, node_width=4)
-    b.build()
-    n = 1 << 18
-    soa = F.gen_rays(ctx, n, 101)
-    rays = F.Rays.from_soa(soa, tmin=1e-4)
-    rc, _ = _noalloc(ctx, b, rays, n)  # outside any capture
-    assert rc == _lib.FLG_OK
-    ctx.sync()
-    s = torch.cuda.Stream()
-    ctx2 = F.Context(0, s)
-    out = {"prim": torch.empty(n, dtype=torch.int32, device="cuda"),
-           "t": torch.empty(n, dtype=torch.float32, device="cuda"),
-           "u": torch.empty(n, dtype=torch.float32, device="cuda"),
-           "v": torch.empty(n, dtype=torch.float32, device="cuda")}
-    r, hs = rays.struct(), F._hits_struct(out)
-    g = C.c_void_p()
-    torch.cuda.synchronize()
-    with torch.cuda.stream(s):
-        ctx2.check(ctx2.lib.flg_graph_begin(ctx2.h))
-        rc = ctx2.lib.flg_trace_closest_noalloc(ctx2.h, b.h, C.byref(r), n, C.byref(hs))
-        ctx2.check(ctx2.lib.flg_graph_end(ctx2.h, C.byref(g)))
-    assert rc == _lib.FLG_OK
-    for trial in range(2):
-        soa.copy_(F.gen_rays(ctx, n, 200 + trial))
-        torch.cuda.synchronize()
-        ctx2.check(ctx2.lib.flg_graph_launch(ctx2.h, g))
-        ctx2.sync()
-        ref = b.intersect(rays)
-        ctx.sync()
-        for k in ("prim", "t", "u", "v"):
-            assert torch.equal(out[k], ref[k]), (trial, k)
-        assert float((out["prim"] >= 0).float().mean()) > 0.3
-    ctx2.lib.flg_graph_destroy(g)
-    ctx2.close()
 
 
 def test_noalloc_first_call_inside_a_capture_is_refused():
