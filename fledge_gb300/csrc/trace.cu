@@ -1051,9 +1051,12 @@ FLG_API int flg_trace_closest_batched(flg_ctx ctx, flg_bvh bvh, const flg_rays *
   return trace_enqueue(ctx, ctx->stream, 0, bvh, rays, n, opts, ctx->d_ray_off, ns, out, nullptr);
 }
 
-// Host-buffer entry point: chunks of rays are staged through device buffers
-// on two streams so that host->device copies, traversal and device->host
-// copies of neighbouring chunks overlap.
+// Host-buffer entry point: chunks of rays are staged through two device
+// buffers.  Every copy runs on the copy stream, in the order H0 H1 D0 H2 D1
+// H3 ... (Hi: chunk i's rays in, Di: its hits out, once its trace on the
+// context's stream is done), so copies overlap the traces but never each
+// other: a host-to-device and a device-to-host copy that run at once each
+// drop to about a third of their bandwidth alone.
 FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *rh, int64_t n,
                                    const flg_trace_opts *opts, flg_hits *oh) {
   if (!ctx || !bvh || !oh) return ctx ? set_error(ctx, FLG_ERR_ARG, "NULL argument") : FLG_ERR_ARG;
@@ -1075,32 +1078,51 @@ FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *rh,
     FLG_CUDA(ctx, cudaMalloc(&ctx->stage, 2 * per_buf));
     ctx->stage_bytes = 2 * per_buf;
   }
-  cudaStream_t ss[2] = {ctx->stream, ctx->copy_stream};
-  // The second stream must not start before earlier work on the main stream.
-  FLG_CUDA(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
-  FLG_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev[0], 0));
-  for (int64_t c0 = 0, ci = 0; c0 < n; c0 += chunk, ++ci) {
-    const int k = (int)(ci & 1);
-    const int64_t m = std::min(chunk, n - c0);
-    cudaStream_t st = ss[k];
+  cudaStream_t cs = ctx->stream, cp = ctx->copy_stream;
+  cudaEvent_t *in_done = ctx->ev, *traced = ctx->ev + 2;  // per buffer
+  // The copy stream must not start before earlier work on the context's stream.
+  FLG_CUDA(ctx, cudaEventRecord(traced[0], cs));
+  FLG_CUDA(ctx, cudaStreamWaitEvent(cp, traced[0], 0));
+  const int64_t n_chunks = (n + chunk - 1) / chunk;
+  auto buffers = [&](int k, float *(&arr)[12]) {
     float *base = (float *)((char *)ctx->stage + k * per_buf);
-    float *arr[12];
     for (int a = 0; a < 12; ++a) arr[a] = base + (size_t)a * chunk;
+  };
+  auto copy_in = [&](int64_t ci) -> int {
+    const int k = (int)(ci & 1);
+    const int64_t c0 = ci * chunk, m = std::min(chunk, n - c0);
+    float *arr[12];
+    buffers(k, arr);
     const float *src[8] = {rh->ox, rh->oy, rh->oz, rh->dx, rh->dy, rh->dz, rh->tmin, rh->tmax};
     for (int a = 0; a < 8; ++a)
-      if (src[a]) FLG_CUDA(ctx, cudaMemcpyAsync(arr[a], src[a] + c0, sizeof(float) * m, cudaMemcpyHostToDevice, st));
+      if (src[a]) FLG_CUDA(ctx, cudaMemcpyAsync(arr[a], src[a] + c0, sizeof(float) * m, cudaMemcpyHostToDevice, cp));
+    FLG_CUDA(ctx, cudaEventRecord(in_done[k], cp));
+    return FLG_OK;
+  };
+  if ((rc = copy_in(0))) return rc;
+  if (n_chunks > 1 && (rc = copy_in(1))) return rc;
+  for (int64_t ci = 0; ci < n_chunks; ++ci) {
+    const int k = (int)(ci & 1);
+    const int64_t c0 = ci * chunk, m = std::min(chunk, n - c0);
+    float *arr[12];
+    buffers(k, arr);
     flg_rays dr{arr[0], arr[1], arr[2], arr[3], arr[4], arr[5], rh->tmin ? arr[6] : nullptr,
                 rh->tmax ? arr[7] : nullptr, rh->tmin_const, rh->tmax_const};
     flg_hits dh{(int32_t *)arr[8], arr[9], arr[10], arr[11]};
     flg_trace_opts op{};
     if (opts) op = *opts;
     op.persistent = 0;
-    rc = trace_enqueue(ctx, st, k, bvh, &dr, m, &op, nullptr, 1, &dh, nullptr);
+    FLG_CUDA(ctx, cudaStreamWaitEvent(cs, in_done[k], 0));
+    rc = trace_enqueue(ctx, cs, k, bvh, &dr, m, &op, nullptr, 1, &dh, nullptr);
     if (rc) return rc;
-    FLG_CUDA(ctx, cudaMemcpyAsync(oh->prim + c0, dh.prim, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, st));
-    FLG_CUDA(ctx, cudaMemcpyAsync(oh->t + c0, dh.t, sizeof(float) * m, cudaMemcpyDeviceToHost, st));
-    FLG_CUDA(ctx, cudaMemcpyAsync(oh->u + c0, dh.u, sizeof(float) * m, cudaMemcpyDeviceToHost, st));
-    FLG_CUDA(ctx, cudaMemcpyAsync(oh->v + c0, dh.v, sizeof(float) * m, cudaMemcpyDeviceToHost, st));
+    FLG_CUDA(ctx, cudaEventRecord(traced[k], cs));
+    FLG_CUDA(ctx, cudaStreamWaitEvent(cp, traced[k], 0));
+    FLG_CUDA(ctx, cudaMemcpyAsync(oh->prim + c0, dh.prim, sizeof(int32_t) * m, cudaMemcpyDeviceToHost, cp));
+    FLG_CUDA(ctx, cudaMemcpyAsync(oh->t + c0, dh.t, sizeof(float) * m, cudaMemcpyDeviceToHost, cp));
+    FLG_CUDA(ctx, cudaMemcpyAsync(oh->u + c0, dh.u, sizeof(float) * m, cudaMemcpyDeviceToHost, cp));
+    FLG_CUDA(ctx, cudaMemcpyAsync(oh->v + c0, dh.v, sizeof(float) * m, cudaMemcpyDeviceToHost, cp));
+    // this buffer's next rays: after its hits are out (same stream)
+    if (ci + 2 < n_chunks && (rc = copy_in(ci + 2))) return rc;
   }
   FLG_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
   FLG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -55,6 +55,37 @@ def test_batched_persistent_equals_plain(ctx):
         assert np.array_equal(a[k], b[k]), k
 
 
+def test_back_to_back_traces_with_changing_offsets(ctx):
+    """Batched traces enqueued one after another with different ray offsets
+    and no synchronisation in between (each uploads its offsets on the
+    context's stream): every call sees its own offsets, as when the calls
+    run one at a time."""
+    import fledge_gb300 as F
+    counts = [500, 3000, 20, 7000, 1, 1200]
+    bb, pos, soa, offs, roffs = _batch(ctx, counts, rays_per_tri=6, seed=11)
+    rays = F.Rays.from_soa(soa, tmin=1e-4)
+    n = int(roffs[-1])
+    # the rays split into groups of scenes, each traced with its own offsets
+    groups = [(0, 2), (2, 3), (3, 6)]
+    ref = U.host(bb.intersect_batched(rays, roffs))
+    ctx.sync()
+    outs = []
+    for rep in range(3):
+        for (a, b) in groups:
+            r0, r1 = int(roffs[a]), int(roffs[b])
+            ro = np.zeros(len(counts) + 1, np.int64)
+            ro[a + 1:b + 1] = roffs[a + 1:b + 1] - roffs[a]
+            ro[b + 1:] = ro[b]
+            sub = F.Rays(*[soa[k, r0:r1] for k in range(6)], tmin_const=1e-4)
+            outs.append((r0, r1, bb.intersect_batched(sub, ro)))
+    ctx.sync()
+    for r0, r1, o in outs:
+        h = U.host(o)
+        for k in ref:
+            assert np.array_equal(h[k], ref[k][r0:r1]), (r0, k)
+    assert n == sum(r1 - r0 for r0, r1, _ in outs) // 3
+
+
 def test_graph_capture_rebuild_and_trace(ctx, oracle):
     """Build + trace captured once, replayed after the vertices change in place."""
     import fledge_gb300 as F

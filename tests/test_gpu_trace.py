@@ -158,14 +158,16 @@ def test_empty_and_single_triangle_scenes(ctx, oracle):
 
 
 def test_host_staged_entry_point(ctx, oracle):
-    """flg_trace_closest_host: host buffers in, host buffers out, chunked."""
+    """flg_trace_closest_host: host buffers in, host buffers out, in chunks of
+    2^22 rays through two staging buffers (three chunks: the first buffer is
+    refilled once its hits are out)."""
     import ctypes as C
 
     import fledge_gb300 as F
     import torch
     pos = G.random_soup(30000, np.random.default_rng(61))
     b, _ = U.gpu_build(ctx, pos, width=4)
-    n = (1 << 22) + 12345  # crosses a chunk boundary
+    n = (2 << 22) + 12345
     r8 = G.sphere_rays(n, np.random.default_rng(62))
     rh = torch.from_numpy(r8).pin_memory()
     out = {k: torch.empty(n, dtype=torch.int32 if k == "prim" else torch.float32).pin_memory()
