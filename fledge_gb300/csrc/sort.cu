@@ -5,7 +5,7 @@
 // the sort is stable, so equal codes keep ascending original index.
 //
 // One launch per 8-bit digit.  Each CTA claims a tile of 3072 pairs (256
-// threads x 12) in launch order, ranks its keys with warp match-any and
+// threads x 12) in launch order, ranks its keys with warp ballots and
 // shared-memory atomics, publishes its per-digit counts,
 // resolves its global offsets by looking back over earlier tiles, reorders
 // the tile in shared memory and writes runs of equal digits contiguously.
@@ -47,7 +47,7 @@ __device__ __forceinline__ uint32_t sort_digit(uint32_t key, uint32_t val, int s
 // One pass over one tile.  Phases: (1) each warp loads 32 x kSortItems
 // consecutive pairs (coalesced, no bounds checks on full tiles); (2) ranks
 // them: per item, the lanes holding the same digit find each other with
-// match-any and their lowest lane adds the group's size to the warp's
+// eight ballots and their lowest lane adds the group's size to the warp's
 // counter for that digit with a shared-memory atomic whose old value is the
 // group's base.  The atomics of successive items of a warp are issued back
 // to back (nothing waits for the previous item's counter), and a warp's
@@ -138,7 +138,18 @@ __global__ void __launch_bounds__(kSortThreads, kSortMinBlocks)
   for (int j = 0; j < kSortItems; ++j) {
     const bool valid = full || j * 32 < wrem;
     const uint32_t d = !valid ? 256u : kScene ? dg[kScene ? j : 0] : ((k[j] >> shift) & 0xFFu);
-    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
+    // Lanes holding the same digit: one ballot per digit bit (and one for
+    // validity on a partial tile), about twice as fast as match-any here.
+    uint32_t peers = 0xFFFFFFFFu;
+    if (!full) {
+      const uint32_t m = __ballot_sync(0xFFFFFFFFu, valid);
+      peers = valid ? m : ~m;
+    }
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const uint32_t m = __ballot_sync(0xFFFFFFFFu, (d >> b) & 1u);
+      peers &= ((d >> b) & 1u) ? m : ~m;
+    }
     const int leader = __ffs(peers) - 1;
     uint32_t gbase = 0u;
     if (lane == leader && d < 256u) gbase = atomicAdd(&s_whist[warp][d], (uint32_t)__popc(peers));
