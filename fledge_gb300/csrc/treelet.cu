@@ -47,6 +47,12 @@ __device__ __forceinline__ void tl_merge(TlBox &a, const TlBox &b) {
   }
 }
 
+__device__ __forceinline__ uint32_t tl_arrive(uint32_t *flag) {
+  uint32_t old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(flag) : "memory");
+  return old;
+}
+
 // Subsets of the 7 treelet leaves ordered by size: kTlCount[k] subsets of
 // size k from kTlOffset[k].
 __constant__ uint8_t kTlSubsets[kTlFull] = {
@@ -342,19 +348,23 @@ __global__ void __launch_bounds__(kTlThreads)
     // tree left inconsistent by an earlier timed-out build
     for (int depth = 0; __any_sync(0xffffffffu, x >= 0); ++depth) {
       bool big = false;
+      // The arrival is an acquire-release add: it publishes this lane's
+      // earlier writes (the child it finished) and, for the second arrival,
+      // makes the sibling's visible.
       if (x >= 0) {
-        __threadfence();
-        if (atomicAdd(T.flag + x, 1u) == 0u) {
+        if (tl_arrive(T.flag + x) == 0u) {
           x = -1;
         } else {
           T.flag[x] = 0u;  // both arrivals seen: ready for the next round
-          __threadfence();
           big = T.finish(x) >= gamma;
         }
       }
-      for (unsigned need = __ballot_sync(0xffffffffu, big); need; need &= need - 1)
+      const unsigned need0 = __ballot_sync(0xffffffffu, big);
+      for (unsigned need = need0; need; need &= need - 1)
         T.restructure(__shfl_sync(0xffffffffu, x, __ffs(need) - 1), w, lane);
-      __threadfence();
+      // a rebuilt treelet is written by every lane: visible before its root's
+      // lane arrives at the parent
+      if (need0) __threadfence();
       if (x >= 0) x = depth < 127 ? __ldcg(T.parent + x) : -1;
     }
   }
