@@ -693,6 +693,24 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
                     h_out[k][r0:r1].copy_(d_out[k][r0:r1], non_blocking=True)
         main.wait_stream(copy)
 
+    # Copy rates of this machine, each direction alone (one column of rays in,
+    # one hit array out; outside the timed region): the e2e step hides its
+    # copies behind the traces except the first group in and the last out.
+    def rate(dst, src):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(main)
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        e1.record(main)
+        torch.cuda.synchronize()
+        return round(3 * src.numel() * src.element_size() / (e0.elapsed_time(e1) * 1e6), 1)
+
+    m = min(n_rays, 1 << 28)
+    h2d_gbs = rate(d_rays[0, :m], h_rays[0, :m])
+    d2h_gbs = rate(h_out["t"][:m], d_out["t"][:m])
+
     for _ in range(max(1, args.warmup)):
         e2e_step()
     torch.cuda.synchronize()
@@ -705,7 +723,8 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
     bb.destroy()
     return {"value": round(world * n_rays / dt / 1e6, 2), "unit": "Mrays/s",
             "h2d_bytes_per_step": int(n_tri * 36 + n_rays * 24), "d2h_bytes_per_step": int(n_rays * 16),
-            "ms_per_step": round(dt * 1e3, 3), "host_readback_consistent": ok}
+            "ms_per_step": round(dt * 1e3, 3), "host_readback_consistent": ok,
+            "copy_gbs_alone": {"h2d": h2d_gbs, "d2h": d2h_gbs}, "ray_groups": len(groups)}
 
 
 def _time(torch, fn, reps, stream):
