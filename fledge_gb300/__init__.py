@@ -282,13 +282,19 @@ class BatchedRadixBVHBuilder(RadixBVHBuilder):
                                                  C.byref(h)))
         self.h = h
 
-    def intersect_batched(self, rays: Rays, ray_offsets: Sequence[int], out=None, **opts):
+    def intersect_batched(self, rays: Rays, ray_offsets: Sequence[int], out=None, ctx: Optional[Context] = None,
+                          **opts):
+        """Closest hits of every scene's rays in one launch.  ``ctx``: trace
+        on another context (its stream and scratch) than the one that built
+        the handle; traces only read the handle, so traces on several
+        contexts may run at once, but not beside a rebuild."""
+        c = ctx or self.ctx
         ro = np.ascontiguousarray(np.asarray(ray_offsets, dtype=np.int64))
         n = int(ro[-1])
         out = out or _alloc_hits(n, rays.ox.device)
         r, hs, op = rays.struct(), _hits_struct(out), _trace_opts(**opts)
-        self.ctx.check(self.ctx.lib.flg_trace_closest_batched(
-            self.ctx.h, self.h, C.byref(r), ro.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(op), C.byref(hs)))
+        c.check(c.lib.flg_trace_closest_batched(
+            c.h, self.h, C.byref(r), ro.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(op), C.byref(hs)))
         return out
 
     def topology(self, scene: int = 0, n: Optional[int] = None) -> dict:

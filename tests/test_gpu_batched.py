@@ -86,6 +86,37 @@ def test_back_to_back_traces_with_changing_offsets(ctx):
     assert n == sum(r1 - r0 for r0, r1, _ in outs) // 3
 
 
+def test_traces_on_two_contexts_share_a_handle(ctx):
+    """One handle traced from two contexts (two streams) at once, groups of
+    scenes alternating between them: the hits equal one trace of all rays."""
+    import fledge_gb300 as F
+    counts = [4000, 300, 9000, 1, 2500, 7000, 50]
+    bb, pos, soa, offs, roffs = _batch(ctx, counts, rays_per_tri=6, seed=21)
+    rays = F.Rays.from_soa(soa, tmin=1e-4)
+    ref = U.host(bb.intersect_batched(rays, roffs))
+    ctx.sync()
+    side = torch.cuda.Stream()
+    ctx2 = F.Context(0, side)
+    built = torch.cuda.Event()
+    built.record(ctx.stream)
+    side.wait_event(built)
+    outs = []
+    for gi, (a, b) in enumerate([(0, 1), (1, 3), (3, 4), (4, 7)]):
+        r0, r1 = int(roffs[a]), int(roffs[b])
+        ro = np.zeros(len(counts) + 1, np.int64)
+        ro[a + 1:b + 1] = roffs[a + 1:b + 1] - roffs[a]
+        ro[b + 1:] = ro[b]
+        sub = F.Rays(*[soa[k, r0:r1] for k in range(6)], tmin_const=1e-4)
+        outs.append((r0, r1, bb.intersect_batched(sub, ro, ctx=(ctx, ctx2)[gi & 1])))
+    ctx.sync()
+    ctx2.sync()
+    for r0, r1, o in outs:
+        h = U.host(o)
+        for k in ref:
+            assert np.array_equal(h[k], ref[k][r0:r1]), (r0, k)
+    ctx2.close()
+
+
 def test_graph_capture_rebuild_and_trace(ctx, oracle):
     """Build + trace captured once, replayed after the vertices change in place."""
     import fledge_gb300 as F
