@@ -143,3 +143,44 @@ def sliver_comb(group, rng):
     r[3], r[4], r[5] = 1.0, 0.0, 0.0
     r[6], r[7] = 0.0, np.inf
     return pos.astype(np.float32), r
+
+
+def edge_case_scene(rng):
+    """Triangles and rays at the edges of the arithmetic: a 16 x 16 grid of
+    axis-aligned squares in the plane z = 0.5 (two triangles each, sharing
+    edges and vertices), collinear and single-point triangles, and a random
+    soup; rays straight down through grid vertices and edges, rays in the
+    grid's plane and along the axes, diagonal rays, a zero direction and NaN
+    origins.  Returns (positions [n, 3], rays [8, m])."""
+    tris = []
+    k = 16
+    for i in range(k):
+        for j in range(k):
+            x0, x1, y0, y1 = i / k, (i + 1) / k, j / k, (j + 1) / k
+            tris.append([[x0, y0, 0.5], [x1, y0, 0.5], [x1, y1, 0.5]])
+            tris.append([[x0, y0, 0.5], [x1, y1, 0.5], [x0, y1, 0.5]])
+    tris.append([[0.1, 0.1, 0.2], [0.2, 0.2, 0.2], [0.3, 0.3, 0.2]])  # collinear
+    tris.append([[0.4, 0.4, 0.3], [0.4, 0.4, 0.3], [0.4, 0.4, 0.3]])  # a point
+    tris.append([[0.6, 0.1, 0.8], [0.6, 0.1, 0.8], [0.7, 0.2, 0.8]])  # a segment
+    pos = np.concatenate([np.array(tris, np.float32).reshape(-1, 3), random_soup(1000, rng)])
+    rays = []
+    g = np.arange(k + 1, dtype=np.float32) / np.float32(k)
+    for x in g:  # down through every grid vertex and the midpoints of vertical edges
+        for y in g:
+            rays.append([x, y, 2.0, 0.0, 0.0, -1.0])
+            rays.append([x, y + np.float32(0.5 / k), 2.0, 0.0, 0.0, -1.0])
+    for y in g:  # in the grid's plane and just above and below it, along +x and -y
+        for z in (0.5, np.nextafter(np.float32(0.5), np.float32(1)), np.nextafter(np.float32(0.5), np.float32(0))):
+            rays.append([-1.0, y, z, 1.0, 0.0, 0.0])
+            rays.append([y, 2.0, z, 0.0, -1.0, 0.0])
+    d = rng.normal(size=(512, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    o = np.float32(0.5) - 1.5 * d
+    rays += [list(o[i]) + list(d[i]) for i in range(512)]
+    rays.append([0.5, 0.5, 2.0, 0.0, 0.0, 0.0])  # zero direction
+    rays.append([np.nan, 0.5, 2.0, 0.0, 0.0, -1.0])
+    rays.append([0.5, 0.5, 2.0, np.nan, 0.0, -1.0])
+    r = np.zeros((8, len(rays)), np.float32)
+    r[:6] = np.array(rays, np.float32).T
+    r[6], r[7] = 0.0, np.inf
+    return pos.astype(np.float32), r

@@ -118,6 +118,51 @@ def test_golden_fixture_hits(ctx):
         assert np.array_equal(hs[k], d["sphere_hit_" + k]), k
 
 
+@pytest.mark.parametrize("layout", [(2, 1, {}), (4, 1, {}), (4, 3, {"persistent": 2, "refill_lanes": 16,
+                                                                    "stack_depth": 32}),
+                                    (8, 2, {"persistent": 1, "refill_lanes": 8})], ids=_ids)
+def test_edge_case_rays_match_oracle(ctx, oracle, layout):
+    """Rays through shared vertices and edges of an axis-aligned grid
+    (watertight: every interior one hits), rays in and next to the grid's
+    plane (zero direction components: NaN slabs), degenerate triangles, a
+    zero direction and NaN origins: closest hits and occlusion equal the
+    oracle's."""
+    pos, r8 = G.edge_case_scene(np.random.default_rng(5))
+    tree = oracle.build_bvh(pos)
+    w, leaf, opts = layout
+    b, _ = U.gpu_build(ctx, pos, width=w, leaf=leaf)
+    rd, _ = U.rays_dev(r8)
+    hg = U.host(b.intersect(rd, **opts))
+    ctx.sync()
+    bad, ties, ho = U.compare_closest(oracle, pos, None, tree, r8, hg, oracle.MODE_DEV)
+    # A leaf range is tested once its range box passes the slab test, where
+    # the reference tests each triangle pair's parent box.  A ray through a
+    # vertex shared by flat (zero-thickness) boxes can pass the range box and
+    # fail the tighter parent boxes by one rounding: then the GPU finds a hit
+    # that the reference's traversal misses.  Such a hit must be one the
+    # triangle test accepts at exactly the reported t; nothing else may differ.
+    tri = pos.reshape(-1, 3, 3)
+    extra_rays = np.nonzero((hg["prim"] >= 0) & (ho["prim"] < 0))[0]
+    for i in extra_rays:
+        ok, t = oracle.pluecker(tri[hg["prim"][i], 0], tri[hg["prim"][i], 1], tri[hg["prim"][i], 2],
+                                r8[0:3, i], r8[3:6, i], oracle.MODE_DEV)
+        assert ok and float(t[0]) >= r8[6, i], i
+    extra = len(extra_rays)
+    assert bad - extra == 0, f"{bad - extra} prim mismatches ({ties} exact ties)"
+    assert extra == 0 if leaf == 1 else extra <= 8, extra
+    same = hg["prim"] == ho["prim"]
+    for k in ("t", "u", "v"):
+        assert np.array_equal(hg[k][same], ho[k][same]), k
+    down = 17 * 17 * 2
+    inside = (r8[0, :down] < 1.0) & (r8[1, :down] < 1.0)
+    assert np.all(hg["prim"][:down][inside] >= 0)
+    assert np.all(hg["prim"][-3:] == -1)
+    occ = b.intersectP(rd, **opts).cpu().numpy()
+    ref = oracle.trace_any(pos, None, tree, r8, oracle.MODE_DEV)
+    ref[extra_rays] = 1  # the same rays, occluded by the same accepted hits
+    assert np.array_equal(occ, ref), np.count_nonzero(occ != ref)
+
+
 def test_tmin_tmax_and_constants(ctx, oracle):
     pos = G.random_soup(20000, np.random.default_rng(31), half=0.03)
     tree = oracle.build_bvh(pos)
