@@ -184,3 +184,30 @@ def edge_case_scene(rng):
     r[:6] = np.array(rays, np.float32).T
     r[6], r[7] = 0.0, np.inf
     return pos.astype(np.float32), r
+
+
+def volume_edge_rays(rng):
+    """Rays at the edges of the volume's box arithmetic (box [0, 1]^3):
+    origins inside the box, finite tmax ending inside it, rays in a face's
+    plane and parallel to it (zero direction components), rays just outside a
+    face, rays that miss the box, and NaN origins.  Returns rays [8, m]."""
+    rays = []
+    n = 512
+    o = rng.random((n, 3))
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    for i in range(n):  # inside, unbounded and ending inside
+        rays.append(list(o[i]) + list(d[i]) + [0.0, np.inf])
+        rays.append(list(o[i]) + list(d[i]) + [0.0, 0.1 + 0.3 * float(rng.random())])
+    g = np.linspace(0.0, 1.0, 9, dtype=np.float32)
+    for a in g:  # in the faces' planes x = 0, y = 1, along axes, and just outside x = 0
+        for b in g:
+            rays.append([0.0, a, -0.5, 0.0, 0.0, 1.0, 0.0, np.inf])
+            rays.append([a, 1.0, b - 2.0, 0.0, 0.0, 1.0, 0.0, np.inf])
+            rays.append([-0.5, a, b, 1.0, 0.0, 0.0, 0.0, np.inf])
+            rays.append([np.nextafter(np.float32(0), np.float32(-1)), a, -0.5, 0.0, 0.0, 1.0, 0.0, np.inf])
+    for i in range(64):  # misses
+        rays.append([2.0, 2.0, float(i) / 64, 1.0, 0.0, 0.0, 0.0, np.inf])
+    rays.append([np.nan, 0.5, 0.5, 1.0, 0.0, 0.0, 0.0, np.inf])
+    rays.append([0.5, 0.5, -1.0, 0.0, np.nan, 1.0, 0.0, np.inf])
+    return np.array(rays, np.float32).T.copy()

@@ -71,6 +71,31 @@ def test_sample_matches_oracle(ctx, oracle):
     assert 0.1 < oko.mean() < 0.99
 
 
+def test_volume_edge_rays_match_oracle(ctx, oracle):
+    """Origins inside the box, tmax ending inside it, rays in and parallel
+    to a face's plane (zero direction components), rays just outside a face,
+    misses and NaN origins: T, checkpoints, collisions and the adjoint equal
+    the oracle's."""
+    rho = G.value_noise_grid(32, np.random.default_rng(3))
+    r8 = G.volume_edge_rays(np.random.default_rng(4))
+    v = _vol(ctx, rho)
+    rd, _ = U.rays_dev(r8)
+    T, ck = v.tr(rd, 123, checkpoint=True)
+    To, cko = oracle.volume_tr(rho, [0, 0, 0], [1, 1, 1], Med, r8, 123, want_ckpt=True)
+    assert np.array_equal(T.cpu().numpy(), To)
+    assert np.array_equal(ck["k"].cpu().numpy().view(np.uint32), cko["k"])
+    assert np.array_equal(ck["t"].cpu().numpy(), cko["t"])
+    assert np.all(To[-66:] == 1.0)  # misses and NaN origins see no medium
+    ok, p, w = v.sample(rd, 123)
+    oko, po, wo = oracle.volume_sample(rho, [0, 0, 0], [1, 1, 1], Med, r8, 123)
+    assert np.array_equal(ok.cpu().numpy(), oko)
+    assert np.array_equal(p.cpu().numpy(), po) and np.array_equal(w.cpu().numpy(), wo)
+    dLdT = torch.ones_like(T)
+    g = v.tr_adjoint(rd, 123, dLdT, T, ck).cpu().numpy().astype(np.float64)
+    go = oracle.volume_tr_adjoint(rho, [0, 0, 0], [1, 1, 1], Med, r8, 123, np.ones(r8.shape[1], np.float32))
+    assert np.max(np.abs(g - go)) <= 1e-4 * np.abs(go).max()
+
+
 def test_majorant_is_grid_max(ctx):
     import fledge_gb300 as F
     rho = F.gen_noise_grid(ctx, 40, 5)
