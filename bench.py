@@ -418,6 +418,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                                f"({prof.get('workload')}), scaled by rays" if prof_ok else
                                "none: no committed capture of this kernel's current source"),
             "limiter": prof.get("limiter") if prof_ok else None,
+            # the kernel's own roof: the L1 data pipe (fraction of its wavefronts busy, ncu)
+            "l1_wavefront_frac": round(prof["l1tex_data_pipe_wavefronts_pct"] / 100.0, 4) if prof_ok else None,
             "profile_source_sha16": prof.get("source_sha16"), "source_sha16": source_hash(TRACE_SOURCES)}
     roof["frac"] = round(roof["achieved"] / roof["peak"], 4)
     b_ms = statistics.median(build_ms)
