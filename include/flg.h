@@ -224,8 +224,12 @@ FLG_API int flg_trace_closest_batched(flg_ctx ctx, flg_bvh bvh, const flg_rays *
                                       const flg_trace_opts *opts, flg_hits *out);
 
 /* Same as flg_trace_closest with host (preferably pinned) buffers: the call
- * stages rays to the device in chunks, traces and copies hits back, with
- * copies and kernels overlapped on two streams.  Synchronous. */
+ * stages rays to the device in chunks of 2^22 through two buffers, traces
+ * each chunk on the context's stream and copies its hits back; every copy
+ * runs on the context's copy stream in the order in(0) in(1) out(0) in(2)
+ * out(1) ..., so copies overlap the traces but never each other (a
+ * host-to-device and a device-to-host copy running at once each lose about
+ * two thirds of their bandwidth).  Synchronous. */
 FLG_API int flg_trace_closest_host(flg_ctx ctx, flg_bvh bvh, const flg_rays *rays_host,
                                    int64_t n, const flg_trace_opts *opts, flg_hits *out_host);
 
