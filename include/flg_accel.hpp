@@ -20,13 +20,19 @@
 // reference declares them (ray.h:126-128, interaction.hpp:44-80, sampler.h:
 // 20-23), and to any 3-vector type constructible from three floats with
 // operator[].  Errors throw flg::Error carrying the status and the context's
-// message (the reference aborts instead, debug.hpp:60-69).
+// message (the reference aborts instead, debug.hpp:60-69).  The reference's
+// integrators call intersect / tr / sample from many threads at once
+// (integrator.cpp:194-231): every adapter call holds its Context's mutex
+// (calls share the context's stream and scratch and the adapter's staging
+// buffers), so such calls are safe, one at a time per context; for
+// throughput, batch the rays, or give threads their own contexts.
 #pragma once
 
 #include <cuda_runtime.h>
 
 #include <array>
 #include <cstdint>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -66,9 +72,13 @@ class Context {
   void sync() { check(flg_ctx_sync(h_), h_); }
   flg_ctx get() const { return h_; }
   cudaStream_t stream() const { return (cudaStream_t)flg_ctx_stream(h_); }
+  // Held by every adapter call on this context: a context (its stream,
+  // scratch and error word) serves one call at a time.
+  std::mutex &mutex() const { return mu_; }
 
  private:
   flg_ctx h_ = nullptr;
+  mutable std::mutex mu_;
 };
 
 // Device scratch owned by an adapter, grown on demand.
@@ -147,6 +157,7 @@ class RadixBVHBuilder {
 
   // BVHBuilderBase::build
   void build() {
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     if (h_) {
       check(flg_bvh_rebuild(ctx_.get(), h_, mesh_.p), ctx_.get());
       return;
@@ -156,18 +167,21 @@ class RadixBVHBuilder {
 
   // BVHBuilderBase::getBound: {lower xyz, upper xyz}
   std::array<float, 6> getBound() const {
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     flg_bvh_info info{};
     check(flg_bvh_info_get(h_, &info), ctx_.get());
     return {info.bound[0], info.bound[1], info.bound[2], info.bound[3], info.bound[4], info.bound[5]};
   }
 
   // Closest hit on device arrays.
-  void intersect(const flg_rays &rays, int64_t n, flg_hits &out, const flg_trace_opts *opts = nullptr) {
+  void intersect(const flg_rays &rays, int64_t n, flg_hits &out, const flg_trace_opts *opts = nullptr) const {
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     check(flg_trace_closest(ctx_.get(), h_, &rays, n, opts, &out), ctx_.get());
   }
 
   // Any hit on device arrays.
-  void intersectP(const flg_rays &rays, int64_t n, uint8_t *occluded, const flg_trace_opts *opts = nullptr) {
+  void intersectP(const flg_rays &rays, int64_t n, uint8_t *occluded, const flg_trace_opts *opts = nullptr) const {
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     check(flg_trace_any(ctx_.get(), h_, &rays, n, opts, occluded), ctx_.get());
   }
 
@@ -177,8 +191,9 @@ class RadixBVHBuilder {
   // reference's arithmetic with the Euclidean norm where its StableNormalize
   // adds z for z*z); a miss leaves the record as it was, like the reference.
   // tnear is honoured as the ray's tmin.  Synchronous.
-  void intersect(BVHRayHit *rh, int64_t n) {
+  void intersect(BVHRayHit *rh, int64_t n) const {
     if (n <= 0) return;
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     std::vector<float> soa(8 * (size_t)n);
     for (int64_t i = 0; i < n; ++i) {
       for (int k = 0; k < 3; ++k) {
@@ -219,7 +234,7 @@ class RadixBVHBuilder {
   DeviceMesh mesh_;
   flg_build_opts opts_;
   flg_bvh h_ = nullptr;
-  Staging stage_;
+  mutable Staging stage_;
 };
 
 // The live renderer's acceleration structure (Accel : Primitive, accel.hpp:
@@ -259,6 +274,7 @@ class GpuLBVH {
 
   // Primitive::getBound: {lower xyz, upper xyz}
   std::array<float, 6> getBound() const {
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     flg_bvh_info info{};
     check(flg_bvh_info_get(h_, &info), ctx_.get());
     return {info.bound[0], info.bound[1], info.bound[2], info.bound[3], info.bound[4], info.bound[5]};
@@ -267,7 +283,7 @@ class GpuLBVH {
   // Primitive::intersect for one ray (one trace launch; prefer the batch).
   // prim (optional) receives the hit triangle's index, -1 on a miss, so that
   // a caller can set isect.m_primitive from its own primitive list.
-  bool intersect(const Ray &ray, SInteraction &isect, int32_t *prim = nullptr) {
+  bool intersect(const Ray &ray, SInteraction &isect, int32_t *prim = nullptr) const {
     bool hit = false;
     intersect(&ray, &isect, &hit, 1, prim);
     return hit;
@@ -275,8 +291,9 @@ class GpuLBVH {
 
   // Primitive::intersect for n rays: hit[i] as the one-ray call returns it;
   // prim_out (optional, n entries) the hit triangles.
-  void intersect(const Ray *rays, SInteraction *isect, bool *hit, int64_t n, int32_t *prim_out = nullptr) {
+  void intersect(const Ray *rays, SInteraction *isect, bool *hit, int64_t n, int32_t *prim_out = nullptr) const {
     if (n <= 0) return;
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     std::vector<float> soa(8 * (size_t)n);
     for (int64_t i = 0; i < n; ++i) {
       for (int k = 0; k < 3; ++k) {
@@ -337,7 +354,7 @@ class GpuLBVH {
   std::vector<int32_t> ind_;
   std::vector<float> normals_;
   flg_bvh h_ = nullptr;
-  Staging stage_;
+  mutable Staging stage_;
 };
 
 // Philox stream key of a one-ray volume call, drawn from the caller's
@@ -365,23 +382,27 @@ class DenseGridVolume {
 
   // Volume::tr (ratio tracking) on device arrays: ray i draws from Philox
   // stream (seed, i).
-  void tr(const flg_rays &rays, int64_t n, uint64_t seed, float *T, const flg_tr_ckpt *ckpt = nullptr) {
+  void tr(const flg_rays &rays, int64_t n, uint64_t seed, float *T, const flg_tr_ckpt *ckpt = nullptr) const {
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     check(flg_volume_tr(ctx_.get(), h_, &rays, n, seed, T, ckpt), ctx_.get());
   }
   // Volume::sample (delta tracking) on device arrays.
-  void sample(const flg_rays &rays, int64_t n, uint64_t seed, uint8_t *success, float *p, float *weight) {
+  void sample(const flg_rays &rays, int64_t n, uint64_t seed, uint8_t *success, float *p, float *weight) const {
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     check(flg_volume_sample(ctx_.get(), h_, &rays, n, seed, success, p, weight), ctx_.get());
   }
   void tr_adjoint(const flg_rays &rays, int64_t n, uint64_t seed, const float *dL_dT, const float *T,
-                  const flg_tr_ckpt *ckpt, float *dL_dgrid) {
+                  const flg_tr_ckpt *ckpt, float *dL_dgrid) const {
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     check(flg_volume_tr_adjoint(ctx_.get(), h_, &rays, n, seed, dL_dT, T, ckpt, dL_dgrid), ctx_.get());
   }
 
   // Volume::tr for host rays (Ray: m_o, m_d, m_tMax), ray i on stream
   // (seed, i); T: n floats.  Synchronous.
   template <class Ray>
-  void tr(const Ray *rays, int64_t n, uint64_t seed, float *T) {
+  void tr(const Ray *rays, int64_t n, uint64_t seed, float *T) const {
     if (n <= 0) return;
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     flg_rays r = upload(rays, n);
     float *dT = stage_.t;
     check(flg_volume_tr(ctx_.get(), h_, &r, n, seed, dT, nullptr), ctx_.get());
@@ -392,7 +413,7 @@ class DenseGridVolume {
   // Volume::tr(const Ray&, Sampler&) (volume.hpp:22): transmittance from the
   // ray's origin to ray(m_tMax), as a grey 3-vector; one launch per call.
   template <class Ray, class Sampler>
-  auto tr(const Ray &ray, Sampler &rng) -> std::decay_t<decltype(ray.m_o)> {
+  auto tr(const Ray &ray, Sampler &rng) const -> std::decay_t<decltype(ray.m_o)> {
     using V = std::decay_t<decltype(ray.m_o)>;
     float T = 1.0f;
     tr(&ray, 1, stream_key(rng), &T);
@@ -403,11 +424,14 @@ class DenseGridVolume {
   // 23-24): on a real collision sets success, vi = VInteraction(p, -m_d, g)
   // and returns sigma_s / sigma_t; otherwise success = false and 1.
   template <class Ray, class Sampler, class VInteraction>
-  auto sample(const Ray &ray, Sampler &rng, VInteraction &vi, bool &success) -> std::decay_t<decltype(ray.m_o)> {
+  auto sample(const Ray &ray, Sampler &rng, VInteraction &vi, bool &success) const
+      -> std::decay_t<decltype(ray.m_o)> {
     using V = std::decay_t<decltype(ray.m_o)>;
+    const uint64_t key = stream_key(rng);
+    std::lock_guard<std::mutex> lock(ctx_.mutex());
     flg_rays r = upload(&ray, 1);
     uint8_t *ok = (uint8_t *)stage_.prim;
-    check(flg_volume_sample(ctx_.get(), h_, &r, 1, stream_key(rng), ok, stage_.ng, stage_.u), ctx_.get());
+    check(flg_volume_sample(ctx_.get(), h_, &r, 1, key, ok, stage_.ng, stage_.u), ctx_.get());
     uint8_t okh = 0;
     float pw[4];
     cudaStream_t st = ctx_.stream();
@@ -422,7 +446,7 @@ class DenseGridVolume {
 
  private:
   template <class Ray>
-  flg_rays upload(const Ray *rays, int64_t n) {
+  flg_rays upload(const Ray *rays, int64_t n) const {
     std::vector<float> soa(8 * (size_t)n);
     for (int64_t i = 0; i < n; ++i) {
       for (int k = 0; k < 3; ++k) {
@@ -441,7 +465,7 @@ class DenseGridVolume {
   Context &ctx_;
   float g_;
   flg_grid h_ = nullptr;
-  Staging stage_;
+  mutable Staging stage_;
 };
 
 }  // namespace flg

@@ -10,13 +10,17 @@
 //   grid.bin: int32 res, then res^3 float32 densities over the unit box
 //   out.bin:  accel: n uint8 hit, n float32 tMax, 12 n float32 (m_p, m_ng,
 //             m_ns, m_wo per ray); one-ray calls on the first 64 rays agree
-//             with the batch (else exit 6); volume: n float32 T of the batch
+//             with the batch (else exit 6), also when 8 threads make them at
+//             once on the first 512 rays, as the reference's tile-parallel
+//             integrator does (else exit 7); volume: n float32 T of the batch
 //             (seed 11), then for the first 256 rays: uint64 stream key,
 //             float32 T of tr(ray, sampler), then uint64 key, uint8 success,
 //             3 float32 position, float32 weight of sample(ray, sampler, ...)
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <thread>
 #include <vector>
 
 #include "flg_accel.hpp"
@@ -98,6 +102,24 @@ int main(int argc, char **argv) {
       const bool h = accel.intersect(r, it);
       if (h != hit[i] || r.m_tMax != rays[i].m_tMax) return 6;
       if (h && std::memcmp(&it, &isect[i], sizeof(SInteraction)) != 0) return 6;
+    }
+    {
+      std::atomic<int> bad{0};
+      std::vector<std::thread> pool;
+      const int64_t m = n < 512 ? n : 512;
+      for (int w = 0; w < 8; ++w)
+        pool.emplace_back([&, w] {
+          for (int64_t i = w; i < m; i += 8) {
+            Ray r = rays0[i];
+            SInteraction it;
+            const bool h = accel.intersect(r, it);
+            if (h != hit[i] || r.m_tMax != rays[i].m_tMax ||
+                (h && std::memcmp(&it, &isect[i], sizeof(SInteraction)) != 0))
+              bad.fetch_add(1);
+          }
+        });
+      for (auto &t : pool) t.join();
+      if (bad.load() != 0) return 7;
     }
     for (int64_t i = 0; i < n; ++i) {
       const uint8_t b = hit[i] ? 1 : 0;

@@ -30,7 +30,7 @@ def _compile(tmp_path, name):
     from fledge_gb300 import _build
     lib = _build.build()
     exe = str(tmp_path / name)
-    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", os.path.join(CPP, name + ".cpp"),
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-pthread", os.path.join(CPP, name + ".cpp"),
            "-I" + os.path.join(ROOT, "include"), "-I" + CUDA + "/include", lib, "-L" + CUDA + "/lib64", "-lcudart",
            "-Wl,-rpath," + os.path.dirname(lib), "-Wl,-rpath," + CUDA + "/lib64", "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
