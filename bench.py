@@ -756,6 +756,40 @@ def _time(torch, fn, reps, stream):
     return e0.elapsed_time(e1) / reps
 
 
+def _graph_step(torch, F, ctx, b, pos, rays, hits, topts, dev):
+    """A rebuild + trace step captured once into a CUDA graph
+    (flg_graph_begin / end) and replayed, against the same step issued as
+    plain launches: on a small workload the launches are a visible part of
+    the step."""
+    side = torch.cuda.Stream(dev)
+    ctx2 = F.Context(dev.index or 0, side)
+    r, hs, op = rays.struct(), F._hits_struct(hits), F._trace_opts(**topts)
+    # the first trace on a context allocates its scratch: before the capture
+    ctx2.check(ctx2.lib.flg_trace_closest(ctx2.h, b.h, C.byref(r), rays.n, C.byref(op), C.byref(hs)))
+    ctx2.sync()
+    g = C.c_void_p()
+    with torch.cuda.stream(side):
+        ctx2.check(ctx2.lib.flg_graph_begin(ctx2.h))
+        ctx2.check(ctx2.lib.flg_bvh_rebuild(ctx2.h, b.h, C.c_void_p(pos.data_ptr())))
+        ctx2.check(ctx2.lib.flg_trace_closest(ctx2.h, b.h, C.byref(r), rays.n, C.byref(op), C.byref(hs)))
+        ctx2.check(ctx2.lib.flg_graph_end(ctx2.h, C.byref(g)))
+
+    def plain():
+        ctx2.check(ctx2.lib.flg_bvh_rebuild(ctx2.h, b.h, C.c_void_p(pos.data_ptr())))
+        ctx2.check(ctx2.lib.flg_trace_closest(ctx2.h, b.h, C.byref(r), rays.n, C.byref(op), C.byref(hs)))
+
+    res = {}
+    for name, fn in (("graph", lambda: ctx2.check(ctx2.lib.flg_graph_launch(ctx2.h, g))), ("plain", plain)):
+        fn()
+        torch.cuda.synchronize()
+        res[name + "_step_ms"] = round(_time(torch, fn, 50, side), 4)
+    ctx2.sync()
+    ctx2.lib.flg_graph_destroy(g)
+    ctx2.close()
+    res["launches_per_step"] = "build (about 14 kernels) + trace (3), one graph launch when replayed"
+    return res
+
+
 def run_c0(ctx, torch, F, dev, pk):
     """Config 0: 65,536 triangles, 1,048,576 rays: build ms and closest-hit
     Mrays/s for the plain BVH2 kernel and the 4-wide kernel."""
@@ -776,6 +810,8 @@ def run_c0(ctx, torch, F, dev, pk):
         out[f"w{w}"] = {"build_ms": round(bms, 4), "trace_ms": round(tms, 4),
                         "mrays_s": round((1 << 20) / (tms * 1e-3) / 1e6, 1)}
         keep[w] = (b.topology(), {k: v.cpu().numpy() for k, v in hits.items()})
+        if w == 4:
+            out["w4_graph"] = _graph_step(torch, F, ctx, b, pos, rays, hits, topts, dev)
         b.destroy()
     out["build_roofline_frac"] = round(65536 * BYTES_PER_TRI / (out["w2"]["build_ms"] * 1e-3) / 1e9
                                        / pk["hbm_gbs"], 4)
