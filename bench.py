@@ -631,9 +631,18 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
         for line in f:
             if line.startswith("MemAvailable:"):
                 avail = int(line.split()[1]) * 1024
-    if need > 0.6 * avail:
-        return {"value": None, "unit": "Mrays/s", "skipped": f"needs {need / 1e9:.0f} GB pinned host memory, "
-                                                             f"{avail / 1e9:.0f} GB available"}
+    # every rank of this node pins its own copy; all ranks decide together
+    ranks_here = int(os.environ.get("LOCAL_WORLD_SIZE", "1"))
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+    fits = torch.tensor([1 if need * ranks_here <= 0.6 * avail else 0], device=dev)
+    if dist:
+        tdist.all_reduce(fits, op=tdist.ReduceOp.MIN)
+    if int(fits.item()) == 0:
+        return {"value": None, "unit": "Mrays/s",
+                "skipped": f"needs {need * ranks_here / 1e9:.0f} GB pinned host memory for {ranks_here} rank(s), "
+                           f"{avail / 1e9:.0f} GB available"}
     h_pos = torch.empty(pos.shape, dtype=torch.float32, pin_memory=True)
     h_pos.copy_(pos)
     h_rays = torch.empty(soa.shape, dtype=torch.float32, pin_memory=True)
@@ -734,6 +743,10 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
         e2e_step()
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / args.steps
+    if dist:  # the whole job's step: the slowest rank
+        t = torch.tensor([dt], device=dev, dtype=torch.float64)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        dt = float(t.item())
     ok = bool(torch.equal(h_out["prim"][:1 << 20].to(dev), d_out["prim"][:1 << 20]))
     bb.destroy()
     ctx2.close()
