@@ -126,7 +126,8 @@ def test_edge_case_rays_match_oracle(ctx, oracle, layout):
     (watertight: every interior one hits), rays in and next to the grid's
     plane (zero direction components: NaN slabs), degenerate triangles, a
     zero direction and NaN origins: closest hits and occlusion equal the
-    oracle's."""
+    oracle's, but for the extra hits that leaf ranges find at flat-box
+    vertices (below)."""
     pos, r8 = G.edge_case_scene(np.random.default_rng(5))
     tree = oracle.build_bvh(pos)
     w, leaf, opts = layout
