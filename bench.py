@@ -510,8 +510,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     hq = sah = tl = None
     if not args.skip_hq:
         res = {}
-        for name in ("ploc", "sah", "treelet"):
-            hb = F.BatchedRadixBVHBuilder(mesh, offs, ctx, node_width=width, leaf_size=leaf, builder=name)
+        for name, rounds in (("ploc", 0), ("sah", 0), ("treelet", 3), ("treelet1", 1)):
+            hb = F.BatchedRadixBVHBuilder(mesh, offs, ctx, node_width=width, leaf_size=leaf,
+                                          builder=name.rstrip("1"), treelet_rounds=rounds)
             hb.build()
             hb.intersect_batched(rays, roffs, out=hits, **topts)  # warm-up
             torch.cuda.synchronize()
@@ -531,7 +532,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             torch.cuda.synchronize()
             ht_ms = ev[1].elapsed_time(ev[2])
             res[name] = {"builder": {"ploc": "ploc (radius 16)", "sah": "binned SAH (16 buckets, reference rule)",
-                                     "treelet": "LBVH + 3 rounds of 7-leaf treelet restructuring"}[name],
+                                     "treelet": "LBVH + 3 rounds of 7-leaf treelet restructuring",
+                                     "treelet1": "LBVH + 1 round of 7-leaf treelet restructuring"}[name],
                          "build_ms": round(hb_ms, 3), "trace_ms": round(ht_ms, 2),
                          "mrays_s": round(n_rays / (ht_ms * 1e-3) / 1e6, 1),
                          "trace_speedup_vs_lbvh": round(statistics.median(trace_ms) / ht_ms, 3),
@@ -540,6 +542,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             hb.destroy()
             log(f'{name} builder done')
         hq, sah, tl = res["ploc"], res["sah"], res["treelet"]
+        tl["one_round"] = res["treelet1"]
 
 
     # ---- the other workloads ----

@@ -169,13 +169,17 @@ class RadixBVHBuilder:
     """GPU Karras LBVH with the BVHBuilderBase interface (base_bvh.hpp:105-117)."""
 
     def __init__(self, mesh: InternalTriangleMesh, ctx: Optional[Context] = None, node_width: int = 4,
-                 leaf_size: int = 1, builder: str = "lbvh"):
+                 leaf_size: int = 1, builder: str = "lbvh", treelet_rounds: int = 0):
         self.mesh = mesh
         self.ctx = ctx or Context(mesh.p.device.index or 0)
         self.node_width = node_width
         self.leaf_size = leaf_size
         self.builder = _builder_id(builder)
+        self.treelet_rounds = treelet_rounds  # builder 'treelet': passes, 1..4 (0 = 3)
         self.h = None
+
+    def _opts(self) -> FlgBuildOpts:
+        return FlgBuildOpts(self.node_width, self.leaf_size, 1, self.builder, self.treelet_rounds)
 
     def build(self) -> None:
         lib = self.ctx.lib
@@ -183,7 +187,7 @@ class RadixBVHBuilder:
             self.ctx.check(lib.flg_bvh_rebuild(self.ctx.h, self.h, C.c_void_p(_ptr(self.mesh.p))))
             return
         h = C.c_void_p()
-        opts = FlgBuildOpts(self.node_width, self.leaf_size, 1, self.builder)
+        opts = self._opts()
         self.ctx.check(lib.flg_bvh_build(self.ctx.h, C.c_void_p(_ptr(self.mesh.p)),
                                          C.c_void_p(_ptr(self.mesh.ind)), self.mesh.n_tri,
                                          self.mesh.n_vert, C.byref(opts), C.byref(h)))
@@ -264,8 +268,8 @@ class BatchedRadixBVHBuilder(RadixBVHBuilder):
     """Many scenes built in one segmented launch and traced in one launch."""
 
     def __init__(self, mesh: InternalTriangleMesh, tri_offsets: Sequence[int], ctx: Optional[Context] = None,
-                 node_width: int = 4, leaf_size: int = 1, builder: str = "lbvh"):
-        super().__init__(mesh, ctx, node_width, leaf_size, builder)
+                 node_width: int = 4, leaf_size: int = 1, builder: str = "lbvh", treelet_rounds: int = 0):
+        super().__init__(mesh, ctx, node_width, leaf_size, builder, treelet_rounds)
         self.tri_offsets = np.ascontiguousarray(np.asarray(tri_offsets, dtype=np.int64))
 
     def build(self) -> None:
@@ -274,7 +278,7 @@ class BatchedRadixBVHBuilder(RadixBVHBuilder):
             self.ctx.check(lib.flg_bvh_rebuild(self.ctx.h, self.h, C.c_void_p(_ptr(self.mesh.p))))
             return
         h = C.c_void_p()
-        opts = FlgBuildOpts(self.node_width, self.leaf_size, 1, self.builder)
+        opts = self._opts()
         offs = self.tri_offsets.ctypes.data_as(C.POINTER(C.c_int64))
         self.ctx.check(lib.flg_bvh_build_batched(self.ctx.h, C.c_void_p(_ptr(self.mesh.p)),
                                                  C.c_void_p(_ptr(self.mesh.ind)), offs,

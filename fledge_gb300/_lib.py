@@ -28,7 +28,7 @@ class FlgHits(C.Structure):
 
 class FlgBuildOpts(C.Structure):
     _fields_ = [("node_width", C.c_int32), ("leaf_size", C.c_int32), ("keep_topology", C.c_int32),
-                ("builder", C.c_int32)]
+                ("builder", C.c_int32), ("treelet_rounds", C.c_int32)]
 
 
 FLG_BUILDER_LBVH, FLG_BUILDER_PLOC, FLG_BUILDER_SAH, FLG_BUILDER_TREELET = 0, 1, 2, 3

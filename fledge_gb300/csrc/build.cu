@@ -546,6 +546,9 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
       builder != FLG_BUILDER_TREELET)
     return set_error(ctx, FLG_ERR_ARG,
                      "builder must be FLG_BUILDER_LBVH, FLG_BUILDER_PLOC, FLG_BUILDER_SAH or FLG_BUILDER_TREELET");
+  const int tl_rounds = opts && opts->treelet_rounds ? opts->treelet_rounds : 3;
+  if (builder == FLG_BUILDER_TREELET && (tl_rounds < 1 || tl_rounds > 4))
+    return set_error(ctx, FLG_ERR_ARG, "treelet_rounds must be in [1, 4]");
 
   flg_bvh b = new flg_bvh_t();
   b->ctx = ctx;
@@ -558,6 +561,7 @@ static int bvh_create(flg_ctx ctx, const float *pos, const int32_t *idx, const i
   b->leaf_size = leaf_size;
   b->keep_topology = opts ? opts->keep_topology != 0 : true;
   b->builder = builder;
+  b->treelet_rounds = tl_rounds;
   b->tri_off_h.assign(tri_off_host, tri_off_host + n_scenes + 1);
   b->node_off_h.resize(n_scenes + 1);
   b->node_off_h[0] = 0;

@@ -136,6 +136,7 @@ struct flg_bvh_t {
   // node in the final (depth-first) triangle order, used by the collapse, and
   // the clustering scratch (ping-pong cluster arrays, scan buffers, queues).
   int32_t builder = 0;
+  int32_t treelet_rounds = 3;  // FLG_BUILDER_TREELET: restructuring passes
   int32_t *d_rfirst = nullptr, *d_rcount = nullptr;
   float4 *d_cbox[2] = {nullptr, nullptr};  // 2 per cluster: lo, hi
   int32_t *d_cref[2] = {nullptr, nullptr}, *d_ccnt[2] = {nullptr, nullptr}, *d_cscene[2] = {nullptr, nullptr};

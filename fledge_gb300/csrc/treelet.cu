@@ -5,8 +5,8 @@
 // refinement that trades build time for trace speed.
 //
 // After the Karras build (k_climb) the node records are turned into a working
-// form (children, parents, leaf counts, boxes, SAH costs).  Each of three
-// rounds is one bottom-up pass with arrival counters, as the refit: the
+// form (children, parents, leaf counts, boxes, SAH costs).  Each round (3 by
+// default, 1 to 4) is one bottom-up pass with arrival counters, as the refit: the
 // second child to arrive finishes a node (box, count, cost
 // Ci A + C(left) + C(right), A = dx dy + dy dz + dz dx) and, when its
 // subtree holds at least 7 << round triangles, rebuilds the treelet of its 7
@@ -29,7 +29,6 @@ namespace flg {
 
 constexpr float kTlCi = 1.2f, kTlCt = 1.0f;
 constexpr int kTreelet = 7, kTlFull = (1 << kTreelet) - 1;
-constexpr int kTlRounds = 3;
 constexpr int kTlThreads = 128;
 
 struct TlBox {
@@ -488,7 +487,7 @@ int treelet_build(flg_ctx ctx, flg_bvh b) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_tl_round, kTlThreads, 0) != cudaSuccess || v < 1) v = 1;
     return v;
   }();
-  for (int r = 0; r < kTlRounds; ++r) {
+  for (int r = 0; r < b->treelet_rounds; ++r) {
     k_tl_round<<<grid_for(n, kTlThreads, (int64_t)ctx->num_sms * round_per_sm), kTlThreads, 0, st>>>(
         n, kTreelet << r, T);
     FLG_LAUNCH_CHECK(ctx, "k_tl_round");

@@ -77,6 +77,8 @@ typedef struct flg_build_opts {
   int32_t keep_topology;  /* unused: flg_bvh_download derives the Karras arrays from the nodes */
   int32_t builder;        /* FLG_BUILDER_LBVH (0, the Karras radix tree), FLG_BUILDER_PLOC,
                              FLG_BUILDER_SAH or FLG_BUILDER_TREELET */
+  int32_t treelet_rounds; /* FLG_BUILDER_TREELET: restructuring passes, 1..4 (0 = 3); other
+                             builders ignore it */
 } flg_build_opts;
 
 /* Tree builders.  FLG_BUILDER_PLOC is a high-quality alternative to the
@@ -96,12 +98,15 @@ typedef struct flg_build_opts {
  * flg_bvh_download returns its topology (morton is not filled).  One host
  * synchronisation per tree level (not capturable).
  * FLG_BUILDER_TREELET is the LBVH refined by treelet restructuring (Karras &
- * Aila 2013): three bottom-up passes, each rebuilding the 7-leaf treelet
- * below every node whose subtree holds at least 7, 14, 28 triangles into its
- * topology of least SAH cost (Ci = 1.2, Ct = 1; subset dynamic
- * programming); leaves are then renumbered in depth-first order and nodes in
- * Karras' numbering, so flg_bvh_download returns its topology (morton is not
- * in the new order).  Capturable. */
+ * Aila 2013): treelet_rounds bottom-up passes (3 by default), pass r
+ * rebuilding the 7-leaf treelet below every node whose subtree holds at
+ * least 7 << r triangles into its topology of least SAH cost (Ci = 1.2,
+ * Ct = 1; subset dynamic programming); leaves are then renumbered in
+ * depth-first order and nodes in Karras' numbering, so flg_bvh_download
+ * returns its topology (morton is not in the new order).  Capturable.  Most
+ * of the trace gain comes from the first pass: on 256 scenes of 34.6 M
+ * triangles in all, one pass gave a 4.1 % faster trace for 72 ms of
+ * restructuring, three passes 4.9 % for 183 ms. */
 enum { FLG_BUILDER_LBVH = 0, FLG_BUILDER_PLOC = 1, FLG_BUILDER_SAH = 2, FLG_BUILDER_TREELET = 3 };
 
 typedef struct flg_trace_opts {

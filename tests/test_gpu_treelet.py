@@ -1,5 +1,6 @@
 """GPU treelet restructuring (FLG_BUILDER_TREELET) against the oracle's
-restatement: after the LBVH and three restructuring rounds the leaf order,
+restatement: after the LBVH and three restructuring rounds (or the number
+that treelet_rounds asks for) the leaf order,
 topology (split, leaf flags, range end, parents) and node bounds are
 bit-exact, for single scenes and per scene of a batched build; closest hits
 over every layout equal the oracle's except recorded exact ties; rebuilds
@@ -17,11 +18,12 @@ pytestmark = pytest.mark.gpu
 KEYS = ("perm", "split", "leaf_flags", "range_j", "parent", "leaf_parent", "bounds", "scene_bound")
 
 
-def _build(ctx, pos, ind=None, width=2, leaf=1):
+def _build(ctx, pos, ind=None, width=2, leaf=1, rounds=0):
     import fledge_gb300 as F
     p = U.dev(pos.reshape(-1, 3).astype(np.float32))
     i = None if ind is None else U.dev(ind.reshape(-1, 3).astype(np.int32))
-    b = F.RadixBVHBuilder(F.InternalTriangleMesh(p, i), ctx, node_width=width, leaf_size=leaf, builder="treelet")
+    b = F.RadixBVHBuilder(F.InternalTriangleMesh(p, i), ctx, node_width=width, leaf_size=leaf, builder="treelet",
+                          treelet_rounds=rounds)
     b.build()
     return b, (p, i)
 
@@ -37,6 +39,26 @@ def test_treelet_soup_matches_oracle(ctx, oracle, n):
     pos = G.random_soup(n, np.random.default_rng(300 + n))
     b, _ = _build(ctx, pos)
     _same(b.topology(), oracle.build_bvh_treelet(pos))
+
+
+@pytest.mark.parametrize("rounds", [1, 2, 4])
+def test_treelet_rounds_match_oracle(ctx, oracle, rounds):
+    """treelet_rounds: one, two or four passes (thresholds 7, 14, 28, 56
+    triangles) give the oracle's tree after the same number of passes."""
+    pos = G.random_soup(70000, np.random.default_rng(900 + rounds))
+    b, _ = _build(ctx, pos, rounds=rounds)
+    _same(b.topology(), oracle.build_bvh_treelet(pos, rounds=rounds))
+
+
+@pytest.mark.parametrize("rounds", [-1, 5])
+def test_treelet_rounds_out_of_range_rejected(ctx, rounds):
+    import fledge_gb300 as F
+    from fledge_gb300 import _lib
+    p = U.dev(G.random_soup(100, np.random.default_rng(1)).reshape(-1, 3).astype(np.float32))
+    h = C.c_void_p()
+    opts = F.FlgBuildOpts(4, 1, 1, _lib.FLG_BUILDER_TREELET, rounds)
+    rc = ctx.lib.flg_bvh_build(ctx.h, C.c_void_p(p.data_ptr()), None, 100, 300, C.byref(opts), C.byref(h))
+    assert rc == _lib.FLG_ERR_ARG and not h.value
 
 
 @pytest.mark.parametrize("case", ["sphere", "clusters", "duplicates", "lattice"])
