@@ -680,9 +680,25 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
     # then each group's hits once its trace is done): on this system a
     # host-to-device and a device-to-host copy running at once each drop to
     # ~60 GB/s, against ~200 GB/s alone.
+    # Busy time of the copy stream inside the timed steps: events around
+    # every copy batch (each recorded after the batch's wait, so it spans the
+    # copies alone).  The copies are hidden behind the traces while the host
+    # keeps up; on a shared host their rate varies from run to run.
+    spans, timing = [], [False]
+
+    def timed_copy(fn, kind):
+        if not timing[0]:
+            fn()
+            return
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(copy)
+        fn()
+        e1.record(copy)
+        spans.append((kind, e0, e1))
+
     def e2e_step():
         with torch.cuda.stream(copy):
-            d_pos.copy_(h_pos, non_blocking=True)
+            timed_copy(lambda: d_pos.copy_(h_pos, non_blocking=True), "h2d")
             pos_ev = torch.cuda.Event()
             pos_ev.record(copy)
         main.wait_event(pos_ev)
@@ -696,8 +712,8 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
                 r0, r1 = int(roffs[a]), int(roffs[b])
                 # one contiguous copy per ray column: a strided [6, m] slice
                 # would go through a pageable host temporary (~55 GB/s)
-                for k in range(6):
-                    d_rays[k, r0:r1].copy_(h_rays[k, r0:r1], non_blocking=True)
+                timed_copy(lambda: [d_rays[k, r0:r1].copy_(h_rays[k, r0:r1], non_blocking=True)
+                                    for k in range(6)], "h2d")
                 ev = torch.cuda.Event()
                 ev.record(copy)
                 up.append(ev)
@@ -715,8 +731,8 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
             done.record(ts)
             copy.wait_event(done)
             with torch.cuda.stream(copy):
-                for k in h_out:
-                    h_out[k][r0:r1].copy_(d_out[k][r0:r1], non_blocking=True)
+                timed_copy(lambda: [h_out[k][r0:r1].copy_(d_out[k][r0:r1], non_blocking=True)
+                                    for k in h_out], "d2h")
         main.wait_stream(side)
         main.wait_stream(copy)
 
@@ -743,11 +759,17 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
     for _ in range(max(1, args.warmup)):
         e2e_step()
     torch.cuda.synchronize()
+    timing[0] = True
     t0 = time.perf_counter()
     for _ in range(args.steps):
         e2e_step()
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / args.steps
+    timing[0] = False
+    busy = {"h2d": 0.0, "d2h": 0.0}
+    for kind, e0, e1 in spans:
+        busy[kind] += e0.elapsed_time(e1) / args.steps
+    h2d_b, d2h_b = n_tri * 36 + n_rays * 24, n_rays * 16
     if dist:  # the whole job's step: the slowest rank
         t = torch.tensor([dt], device=dev, dtype=torch.float64)
         tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
@@ -758,6 +780,9 @@ def run_e2e(args, ctx, torch, F, pos, soa, offs, roffs, n_tri, n_rays, width, le
     return {"value": round(world * n_rays / dt / 1e6, 2), "unit": "Mrays/s",
             "h2d_bytes_per_step": int(n_tri * 36 + n_rays * 24), "d2h_bytes_per_step": int(n_rays * 16),
             "ms_per_step": round(dt * 1e3, 3), "host_readback_consistent": ok,
+            "copy_stream_in_step": {"h2d_ms": round(busy["h2d"], 1), "d2h_ms": round(busy["d2h"], 1),
+                                    "h2d_gbs": round(h2d_b / (busy["h2d"] * 1e6), 1) if busy["h2d"] else None,
+                                    "d2h_gbs": round(d2h_b / (busy["d2h"] * 1e6), 1) if busy["d2h"] else None},
             "copy_gbs_alone": {"h2d_first_gb": h2d_gbs, "h2d_last_gb": h2d_last_gbs, "d2h_first_gb": d2h_gbs,
                                "d2h_last_gb": d2h_last_gbs}, "ray_groups": len(groups)}
 
