@@ -6,16 +6,19 @@
 //
 // After the Karras build (k_climb) the node records are turned into a working
 // form (children, parents, leaf counts, boxes, SAH costs).  Each round (3 by
-// default, 1 to 4) is one bottom-up pass with arrival counters, as the refit: the
-// second child to arrive finishes a node (box, count, cost
-// Ci A + C(left) + C(right), A = dx dy + dy dz + dz dx) and, when its
-// subtree holds at least 7 << round triangles, rebuilds the treelet of its 7
-// largest descendants (the treelet leaf of largest area is opened until 7
-// leaves; ties to the first in list order) into the topology of least SAH
-// cost by dynamic programming over the 127 subsets of the treelet's leaves
-// (splits holding the lowest member, enumerated from S - 1 downwards, first
-// minimum kept).  A node is finished only after its subtree, so the result
-// does not depend on scheduling.  Nothing waits: the first arrival stops.
+// default, 1 to 4) finishes every node (box, count, cost
+// Ci A + C(left) + C(right), A = dx dy + dy dz + dz dx) after its whole
+// subtree and, when the subtree holds at least 7 << round triangles, rebuilds
+// the treelet of its 7 largest descendants (the treelet leaf of largest area
+// is opened until 7 leaves; ties to the first in list order) into the
+// topology of least SAH cost by dynamic programming over the 127 subsets of
+// the treelet's leaves (splits holding the lowest member, enumerated from
+// S - 1 downwards, first minimum kept).  The order is by height: a pass from
+// the leaves gives every node the height of its subtree, then one launch per
+// height finishes (and rebuilds) the nodes of that height.  Nodes of one
+// height lie in disjoint subtrees, and everything below them was finished by
+// earlier launches, so the result does not depend on scheduling and no fence
+// or arrival protocol is needed.
 // Then every node finds its first leaf in depth-first order by climbing to
 // its root, the leaves and triangle records are regathered in that order and
 // the node records are rewritten in Karras' numbering (root at the scene's
@@ -46,11 +49,9 @@ __device__ __forceinline__ void tl_merge(TlBox &a, const TlBox &b) {
   }
 }
 
-__device__ __forceinline__ uint32_t tl_arrive(uint32_t *flag) {
-  uint32_t old;
-  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(flag) : "memory");
-  return old;
-}
+// Heights are below this bound: a valid tree is at most 62 levels deep
+// after the LBVH build, and a round rebuilds treelets of 7 leaves.
+constexpr int kTlMaxHeight = 128;
 
 // Subsets of the 7 treelet leaves ordered by size: kTlCount[k] subsets of
 // size k from kTlOffset[k].
@@ -106,7 +107,7 @@ struct TlWarp {
 // coherent across SMs.
 struct Tl {
   int32_t *left, *right, *parent, *nleaf, *first, *slot;
-  uint32_t *flag;
+  uint32_t *hw;  // per node: both children's heights + 1 and arrival bits; then the tallest root's
   float *cost;
   float4 *box;  // 2 per node: lo.xyz, hi.xyz
   int32_t *lpar, *lpos;
@@ -316,7 +317,6 @@ __global__ void __launch_bounds__(256)
     const int64_t toff = tri_off[s], n = tri_off[s + 1] - toff;
     if (g >= toff + n - 1) continue;  // a scene's last slot is unused
     const int4 d = nodes[g].d;
-    T.flag[g] = 0u;
     // only a build whose bounded waits gave up leaves refs outside the scene
     if (!tl_ref_ok(d.x, toff, n) || !tl_ref_ok(d.y, toff, n)) {
       atomicOr(err, kErrTimeout);
@@ -330,42 +330,57 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// One round: a thread per leaf climbs; the second arrival at a node finishes
-// it.  Nodes whose subtree is large enough are then rebuilt by the whole
-// warp, one after the other: the nodes that one warp finishes in one step
-// lie in disjoint subtrees (a node is finished only after its whole
-// subtree), so their order does not matter.
+// Height of every node (a leaf's is 0) for the order of a round.  A thread
+// per leaf climbs; each child ORs its height + 1 and its side's bit into the
+// parent's word (bits 0-7 and 16 from the left child, 8-15 and 17 from the
+// right); the second arrival reads its sibling's height from the value the
+// OR returns and climbs on with the larger.  Everything travels in the
+// atomic word, so relaxed atomics suffice.  The threads that finish a root
+// raise `maxh`.
+__global__ void __launch_bounds__(256)
+    k_tl_height(int64_t n_tri, Tl T, uint32_t *hw, uint32_t *maxh) {
+  for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n_tri;
+       pos += (int64_t)gridDim.x * blockDim.x) {
+    int32_t c = ~(int32_t)pos, x = __ldcg(T.lpar + pos);
+    uint32_t h = 0;
+    bool root = false;
+    for (int depth = 0; x >= 0 && depth < kTlMaxHeight - 1; ++depth) {
+      const bool lft = __ldcg(T.left + x) == c;
+      const uint32_t old = atomicOr(hw + x, lft ? ((h + 1) | 0x10000u) : (((h + 1) << 8) | 0x20000u));
+      if (!(old & (lft ? 0x20000u : 0x10000u))) break;  // first arrival
+      h = max(h + 1, lft ? (old >> 8) & 0xFFu : old & 0xFFu);
+      const int32_t p = __ldcg(T.parent + x);
+      if (p < 0) {
+        root = true;
+        break;
+      }
+      c = x;
+      x = p;
+    }
+    if (root) atomicMax(maxh, h);
+  }
+}
+
+// One height of a round: every node of height h is finished; those whose
+// subtree holds >= gamma triangles are then rebuilt by the whole warp, one
+// after the other.  Children were finished by earlier launches.
 __global__ void __launch_bounds__(kTlThreads)
-    k_tl_round(int64_t n_tri, int32_t gamma, Tl T) {
+    k_tl_wave(int64_t n_nodes, uint32_t h, int32_t gamma, Tl T, const uint32_t *__restrict__ hw,
+              const uint32_t *__restrict__ maxh) {
+  if (h > *maxh) return;
   __shared__ TlWarp warps[kTlThreads / 32];
   TlWarp &w = warps[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n_tri;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n_nodes;
        base += (int64_t)gridDim.x * blockDim.x) {
-    int32_t x = base + lane < n_tri ? __ldcg(T.lpar + base + lane) : -1;
-    // a valid tree is at most 62 levels deep; the bound only matters for a
-    // tree left inconsistent by an earlier timed-out build
-    for (int depth = 0; __any_sync(0xffffffffu, x >= 0); ++depth) {
-      bool big = false;
-      // The arrival is an acquire-release add: it publishes this lane's
-      // earlier writes (the child it finished) and, for the second arrival,
-      // makes the sibling's visible.
-      if (x >= 0) {
-        if (tl_arrive(T.flag + x) == 0u) {
-          x = -1;
-        } else {
-          T.flag[x] = 0u;  // both arrivals seen: ready for the next round
-          big = T.finish(x) >= gamma;
-        }
-      }
-      const unsigned need0 = __ballot_sync(0xffffffffu, big);
-      for (unsigned need = need0; need; need &= need - 1)
-        T.restructure(__shfl_sync(0xffffffffu, x, __ffs(need) - 1), w, lane);
-      // a rebuilt treelet is written by every lane: visible before its root's
-      // lane arrives at the parent
-      if (need0) __threadfence();
-      if (x >= 0) x = depth < 127 ? __ldcg(T.parent + x) : -1;
-    }
+    const int64_t g = base + lane;
+    const uint32_t v = g < n_nodes ? hw[g] : 0u;
+    // both children seen (a scene's unused last slot and nodes of an
+    // inconsistent tree keep 0) and this height
+    const bool mine = (v & 0x30000u) == 0x30000u && max(v & 0xFFu, (v >> 8) & 0xFFu) == h;
+    const bool big = mine && T.finish((int32_t)g) >= gamma;
+    for (unsigned need = __ballot_sync(0xffffffffu, big); need; need &= need - 1)
+      T.restructure((int32_t)(base + __ffs(need) - 1), w, lane);
   }
 }
 
@@ -449,7 +464,7 @@ static Tl tl_arrays(flg_bvh b) {
   T.slot = T.first + b->n_nodes;
   T.lpar = T.slot + b->n_nodes;
   T.lpos = T.lpar + b->n_tri;
-  T.flag = b->d_tl_flag;
+  T.hw = b->d_tl_flag;
   T.cost = b->d_tl_cost;
   T.box = b->d_tl_box;
   T.tris = b->d_tris;
@@ -462,7 +477,7 @@ int treelet_reserve(flg_bvh b) {
     if (rc == FLG_OK) rc = halloc(b, p, c);
   };
   A(&b->d_tl_i32, 6 * (size_t)b->n_nodes + 2 * (size_t)b->n_tri);
-  A(&b->d_tl_flag, b->n_nodes);
+  A(&b->d_tl_flag, b->n_nodes + 1);  // heights, then the tallest root's
   A(&b->d_tl_cost, b->n_nodes);
   A(&b->d_tl_box, 2 * (size_t)b->n_nodes);
   A(&b->d_tl_nodes, b->n_nodes);
@@ -482,15 +497,23 @@ int treelet_build(flg_ctx ctx, flg_bvh b) {
   const unsigned g = grid_for(nn, 256, (int64_t)ctx->num_sms * 8);
   k_tl_init<<<g, 256, 0, st>>>(b->d_nodes2, nn, b->d_tri_off, b->n_scenes, T, ctx->d_err);
   FLG_LAUNCH_CHECK(ctx, "k_tl_init");
-  static const int round_per_sm = [] {
+  static const int wave_per_sm = [] {
     int v = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_tl_round, kTlThreads, 0) != cudaSuccess || v < 1) v = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_tl_wave, kTlThreads, 0) != cudaSuccess || v < 1) v = 1;
     return v;
   }();
+  const unsigned gw = grid_for(nn, kTlThreads, (int64_t)ctx->num_sms * wave_per_sm);
   for (int r = 0; r < b->treelet_rounds; ++r) {
-    k_tl_round<<<grid_for(n, kTlThreads, (int64_t)ctx->num_sms * round_per_sm), kTlThreads, 0, st>>>(
-        n, kTreelet << r, T);
-    FLG_LAUNCH_CHECK(ctx, "k_tl_round");
+    // heights of the tree as the previous round left it
+    FLG_CUDA(ctx, cudaMemsetAsync(T.hw, 0, sizeof(uint32_t) * ((size_t)nn + 1), st));
+    k_tl_height<<<grid_for(n, 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(n, T, T.hw, T.hw + nn);
+    FLG_LAUNCH_CHECK(ctx, "k_tl_height");
+    // a fixed launch count keeps the build capturable; heights above the
+    // tallest root return at once
+    for (uint32_t h = 1; h < (uint32_t)kTlMaxHeight; ++h) {
+      k_tl_wave<<<gw, kTlThreads, 0, st>>>(nn, h, kTreelet << r, T, T.hw, T.hw + nn);
+      FLG_LAUNCH_CHECK(ctx, "k_tl_wave");
+    }
   }
   stage_mark(ctx, st, "treelet");
   k_tl_first<<<grid_for(nn + n, 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(nn, n, b->d_tri_off, b->n_scenes, T);

@@ -105,8 +105,8 @@ typedef struct flg_build_opts {
  * depth-first order and nodes in Karras' numbering, so flg_bvh_download
  * returns its topology (morton is not in the new order).  Capturable.  Most
  * of the trace gain comes from the first pass: on 256 scenes of 34.6 M
- * triangles in all, one pass gave a 4.1 % faster trace for 72 ms of
- * restructuring, three passes 4.9 % for 183 ms. */
+ * triangles in all, one pass gave a 4.1 % faster trace for 43 ms of
+ * restructuring, three passes 5.0 % for 86 ms. */
 enum { FLG_BUILDER_LBVH = 0, FLG_BUILDER_PLOC = 1, FLG_BUILDER_SAH = 2, FLG_BUILDER_TREELET = 3 };
 
 typedef struct flg_trace_opts {
