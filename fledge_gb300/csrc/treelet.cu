@@ -107,7 +107,7 @@ struct TlWarp {
 // coherent across SMs.
 struct Tl {
   int32_t *left, *right, *parent, *nleaf, *first, *slot;
-  uint32_t *hw;  // per node: both children's heights + 1 and arrival bits; then the tallest root's
+  uint32_t *hw;  // per node: both children's heights + 1 and arrival bits; then per height counts, starts, cursors
   float *cost;
   float4 *box;  // 2 per node: lo.xyz, hi.xyz
   int32_t *lpar, *lpos;
@@ -335,52 +335,97 @@ __global__ void __launch_bounds__(256)
 // parent's word (bits 0-7 and 16 from the left child, 8-15 and 17 from the
 // right); the second arrival reads its sibling's height from the value the
 // OR returns and climbs on with the larger.  Everything travels in the
-// atomic word, so relaxed atomics suffice.  The threads that finish a root
-// raise `maxh`.
+// atomic word, so relaxed atomics suffice.
 __global__ void __launch_bounds__(256)
-    k_tl_height(int64_t n_tri, Tl T, uint32_t *hw, uint32_t *maxh) {
+    k_tl_height(int64_t n_tri, Tl T, uint32_t *hw) {
   for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n_tri;
        pos += (int64_t)gridDim.x * blockDim.x) {
     int32_t c = ~(int32_t)pos, x = __ldcg(T.lpar + pos);
     uint32_t h = 0;
-    bool root = false;
     for (int depth = 0; x >= 0 && depth < kTlMaxHeight - 1; ++depth) {
       const bool lft = __ldcg(T.left + x) == c;
       const uint32_t old = atomicOr(hw + x, lft ? ((h + 1) | 0x10000u) : (((h + 1) << 8) | 0x20000u));
       if (!(old & (lft ? 0x20000u : 0x10000u))) break;  // first arrival
       h = max(h + 1, lft ? (old >> 8) & 0xFFu : old & 0xFFu);
-      const int32_t p = __ldcg(T.parent + x);
-      if (p < 0) {
-        root = true;
-        break;
-      }
       c = x;
-      x = p;
+      x = __ldcg(T.parent + x);
     }
-    if (root) atomicMax(maxh, h);
+  }
+}
+
+// Height of a node from its word; 0 unless both children arrived (a scene's
+// unused last slot, a node of an inconsistent tree).
+__device__ __forceinline__ uint32_t tl_height(uint32_t v) {
+  return (v & 0x30000u) == 0x30000u ? max(v & 0xFFu, (v >> 8) & 0xFFu) : 0u;
+}
+
+// Nodes listed by height (counting sort; the order within a height does not
+// matter): per-block counts, one global add per height and block.
+// `hc` = count[kTlMaxHeight], start[kTlMaxHeight], cursor[kTlMaxHeight].
+__global__ void __launch_bounds__(256)
+    k_tl_hcount(int64_t n_nodes, const uint32_t *__restrict__ hw, uint32_t *hc) {
+  __shared__ uint32_t cnt[kTlMaxHeight];
+  for (int t = threadIdx.x; t < kTlMaxHeight; t += blockDim.x) cnt[t] = 0u;
+  __syncthreads();
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n_nodes;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t h = tl_height(hw[g]);
+    if (h) atomicAdd(cnt + h, 1u);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kTlMaxHeight; t += blockDim.x)
+    if (cnt[t]) atomicAdd(hc + t, cnt[t]);
+}
+
+__global__ void k_tl_hscan(uint32_t *hc) {
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int h = 0; h < kTlMaxHeight; ++h) {
+      hc[kTlMaxHeight + h] = hc[2 * kTlMaxHeight + h] = run;
+      run += hc[h];
+    }
+  }
+}
+
+// Same slices as k_tl_hcount: a block reserves its range per height with
+// one global add, then places its nodes through shared cursors.
+__global__ void __launch_bounds__(256)
+    k_tl_hplace(int64_t n_nodes, const uint32_t *__restrict__ hw, uint32_t *hc, int32_t *__restrict__ list) {
+  __shared__ uint32_t cnt[kTlMaxHeight];
+  for (int t = threadIdx.x; t < kTlMaxHeight; t += blockDim.x) cnt[t] = 0u;
+  __syncthreads();
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n_nodes;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t h = tl_height(hw[g]);
+    if (h) atomicAdd(cnt + h, 1u);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < kTlMaxHeight; t += blockDim.x)
+    if (cnt[t]) cnt[t] = atomicAdd(hc + 2 * kTlMaxHeight + t, cnt[t]);
+  __syncthreads();
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n_nodes;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t h = tl_height(hw[g]);
+    if (h) list[atomicAdd(cnt + h, 1u)] = (int32_t)g;
   }
 }
 
 // One height of a round: every node of height h is finished; those whose
 // subtree holds >= gamma triangles are then rebuilt by the whole warp, one
-// after the other.  Children were finished by earlier launches.
+// after the other.  Their children were finished by earlier launches.
 __global__ void __launch_bounds__(kTlThreads)
-    k_tl_wave(int64_t n_nodes, uint32_t h, int32_t gamma, Tl T, const uint32_t *__restrict__ hw,
-              const uint32_t *__restrict__ maxh) {
-  if (h > *maxh) return;
+    k_tl_wave(uint32_t h, int32_t gamma, Tl T, const uint32_t *__restrict__ hc, const int32_t *__restrict__ list) {
+  const int64_t m = hc[h], first = hc[kTlMaxHeight + h];
+  if (m == 0) return;
   __shared__ TlWarp warps[kTlThreads / 32];
   TlWarp &w = warps[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n_nodes;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < m;
        base += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t g = base + lane;
-    const uint32_t v = g < n_nodes ? hw[g] : 0u;
-    // both children seen (a scene's unused last slot and nodes of an
-    // inconsistent tree keep 0) and this height
-    const bool mine = (v & 0x30000u) == 0x30000u && max(v & 0xFFu, (v >> 8) & 0xFFu) == h;
-    const bool big = mine && T.finish((int32_t)g) >= gamma;
+    const int32_t x = base + lane < m ? list[first + base + lane] : -1;
+    const bool big = x >= 0 && T.finish(x) >= gamma;
     for (unsigned need = __ballot_sync(0xffffffffu, big); need; need &= need - 1)
-      T.restructure((int32_t)(base + __ffs(need) - 1), w, lane);
+      T.restructure(__shfl_sync(0xffffffffu, x, __ffs(need) - 1), w, lane);
   }
 }
 
@@ -477,7 +522,7 @@ int treelet_reserve(flg_bvh b) {
     if (rc == FLG_OK) rc = halloc(b, p, c);
   };
   A(&b->d_tl_i32, 6 * (size_t)b->n_nodes + 2 * (size_t)b->n_tri);
-  A(&b->d_tl_flag, b->n_nodes + 1);  // heights, then the tallest root's
+  A(&b->d_tl_flag, b->n_nodes + 3 * kTlMaxHeight);  // heights, then counts, starts, cursors per height
   A(&b->d_tl_cost, b->n_nodes);
   A(&b->d_tl_box, 2 * (size_t)b->n_nodes);
   A(&b->d_tl_nodes, b->n_nodes);
@@ -503,15 +548,24 @@ int treelet_build(flg_ctx ctx, flg_bvh b) {
     return v;
   }();
   const unsigned gw = grid_for(nn, kTlThreads, (int64_t)ctx->num_sms * wave_per_sm);
+  const unsigned gn = grid_for(nn, 256, (int64_t)ctx->num_sms * 8);
+  uint32_t *hc = T.hw + nn;
+  int32_t *list = T.first;  // free until k_tl_first
   for (int r = 0; r < b->treelet_rounds; ++r) {
-    // heights of the tree as the previous round left it
-    FLG_CUDA(ctx, cudaMemsetAsync(T.hw, 0, sizeof(uint32_t) * ((size_t)nn + 1), st));
-    k_tl_height<<<grid_for(n, 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(n, T, T.hw, T.hw + nn);
+    // heights of the tree as the previous round left it, nodes listed by height
+    FLG_CUDA(ctx, cudaMemsetAsync(T.hw, 0, sizeof(uint32_t) * ((size_t)nn + 3 * kTlMaxHeight), st));
+    k_tl_height<<<grid_for(n, 256, (int64_t)ctx->num_sms * 8), 256, 0, st>>>(n, T, T.hw);
     FLG_LAUNCH_CHECK(ctx, "k_tl_height");
-    // a fixed launch count keeps the build capturable; heights above the
-    // tallest root return at once
+    k_tl_hcount<<<gn, 256, 0, st>>>(nn, T.hw, hc);
+    FLG_LAUNCH_CHECK(ctx, "k_tl_hcount");
+    k_tl_hscan<<<1, 32, 0, st>>>(hc);
+    FLG_LAUNCH_CHECK(ctx, "k_tl_hscan");
+    k_tl_hplace<<<gn, 256, 0, st>>>(nn, T.hw, hc, list);
+    FLG_LAUNCH_CHECK(ctx, "k_tl_hplace");
+    // a fixed launch count keeps the build capturable; empty heights return
+    // at once
     for (uint32_t h = 1; h < (uint32_t)kTlMaxHeight; ++h) {
-      k_tl_wave<<<gw, kTlThreads, 0, st>>>(nn, h, kTreelet << r, T, T.hw, T.hw + nn);
+      k_tl_wave<<<gw, kTlThreads, 0, st>>>(h, kTreelet << r, T, hc, list);
       FLG_LAUNCH_CHECK(ctx, "k_tl_wave");
     }
   }
