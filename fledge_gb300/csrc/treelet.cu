@@ -412,7 +412,10 @@ __global__ void __launch_bounds__(256)
 
 // One height of a round: every node of height h is finished; those whose
 // subtree holds >= gamma triangles are then rebuilt by the whole warp, one
-// after the other.  Their children were finished by earlier launches.
+// after the other.  Their children were finished by earlier launches.  The
+// list is dealt to the warps round robin (entry i to warp i mod W), so that a
+// short list gives each warp at most one rebuild instead of leaving a few
+// warps with 32 each.
 __global__ void __launch_bounds__(kTlThreads)
     k_tl_wave(uint32_t h, int32_t gamma, Tl T, const uint32_t *__restrict__ hc, const int32_t *__restrict__ list) {
   const int64_t m = hc[h], first = hc[kTlMaxHeight + h];
@@ -420,9 +423,11 @@ __global__ void __launch_bounds__(kTlThreads)
   __shared__ TlWarp warps[kTlThreads / 32];
   TlWarp &w = warps[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < m;
-       base += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t x = base + lane < m ? list[first + base + lane] : -1;
+  const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  for (int64_t k = 0; wid + k * nw < m; k += 32) {
+    const int64_t i = wid + (k + lane) * nw;
+    const int32_t x = i < m ? list[first + i] : -1;
     const bool big = x >= 0 && T.finish(x) >= gamma;
     for (unsigned need = __ballot_sync(0xffffffffu, big); need; need &= need - 1)
       T.restructure(__shfl_sync(0xffffffffu, x, __ffs(need) - 1), w, lane);
