@@ -4,7 +4,8 @@ traversal kernel options of a batched workload, and persists the choice as a
 JSON record that the benchmark loads.
 
 For every builder (the Karras LBVH, PLOC, the binned-SAH rule, the LBVH
-refined by treelet restructuring) the batch is
+refined by three rounds of treelet restructuring, "treelet1" by one round)
+the batch is
 built, the build is timed (median of `reps`), and flg_autotune_trace_batched
 runs its staged search (layout, kernel, block size; each trial the median of
 `reps` launches) on a fraction of every scene's rays.  The builder whose
@@ -55,8 +56,19 @@ def subsample_offsets(ray_offsets, fraction: float):
     return keep, np.concatenate([[0], np.cumsum(keep)]).astype(np.int64)
 
 
+BUILDERS = ("lbvh", "ploc", "sah", "treelet", "treelet1")
+
+
+def builder_args(name: str) -> dict:
+    """Builder keyword arguments of a candidate name: 'treelet<r>' is the
+    treelet builder with r restructuring rounds."""
+    if name.startswith("treelet") and name[7:].isdigit():
+        return {"builder": "treelet", "treelet_rounds": int(name[7:])}
+    return {"builder": name}
+
+
 def tune_batched(ctx: Context, mesh: InternalTriangleMesh, tri_offsets, rays: Rays, ray_offsets,
-                 builders=("lbvh", "ploc", "sah", "treelet"), reps: int = 5, ray_fraction: float = 0.125) -> dict:
+                 builders=BUILDERS, reps: int = 5, ray_fraction: float = 0.125) -> dict:
     """Returns the tuning record (see the module docstring)."""
     torch = _torch()
     ro = np.asarray(ray_offsets, np.int64)
@@ -73,7 +85,7 @@ def tune_batched(ctx: Context, mesh: InternalTriangleMesh, tri_offsets, rays: Ra
     n_full = int(ro[-1])
     per = {}
     for name in builders:
-        bb = BatchedRadixBVHBuilder(mesh, tri_offsets, ctx, node_width=4, leaf_size=1, builder=name)
+        bb = BatchedRadixBVHBuilder(mesh, tri_offsets, ctx, node_width=4, leaf_size=1, **builder_args(name))
         bb.build()
         build_ms = _median_ms(torch, bb.build, reps)
         best = FlgTraceOpts()
@@ -107,7 +119,7 @@ def tune_batched(ctx: Context, mesh: InternalTriangleMesh, tri_offsets, rays: Ra
 
 
 def tune_config3(out: str = DEFAULT_RECORD, reps: int = 5, ray_fraction: float = 0.125,
-                 builders=("lbvh", "ploc", "sah", "treelet")) -> dict:
+                 builders=BUILDERS) -> dict:
     """Tunes the 256-scene batch with the benchmark's seeds and writes the record."""
     torch = _torch()
     from . import gen_rays, gen_triangles
@@ -136,7 +148,7 @@ def main() -> None:
     ap.add_argument("--out", default=DEFAULT_RECORD)
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--ray-fraction", type=float, default=0.125)
-    ap.add_argument("--builders", default="lbvh,ploc,sah,treelet")
+    ap.add_argument("--builders", default=",".join(BUILDERS))
     a = ap.parse_args()
     rec = tune_config3(a.out, a.reps, a.ray_fraction, tuple(a.builders.split(",")))
     print(json.dumps({k: v for k, v in rec.items() if k != "per_builder"}))
