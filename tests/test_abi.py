@@ -94,3 +94,20 @@ def test_builder_ids_match_header():
     assert [F._builder_id(n) for n in ("lbvh", "ploc", "sah", "treelet")] == [0, 1, 2, 3]
     with pytest.raises(ValueError):
         F._builder_id("median")
+
+
+def test_build_opts_layout_and_tuner_candidates():
+    """flg_build_opts in include/flg.h and its ctypes mirror list the same
+    fields in the same order (treelet_rounds last); the tuner's candidate
+    names map to builder arguments ('treelet<r>': r restructuring rounds)."""
+    import fledge_gb300._lib as L
+    from fledge_gb300 import autotune as A
+    text = open(HEADER).read()
+    body = re.search(r"typedef struct flg_build_opts \{(.*?)\} flg_build_opts;", text, re.S).group(1)
+    fields = re.findall(r"int32_t\s+(\w+);", body)
+    assert fields == [f for f, _ in L.FlgBuildOpts._fields_]
+    assert fields[-1] == "treelet_rounds"
+    assert A.builder_args("treelet1") == {"builder": "treelet", "treelet_rounds": 1}
+    assert A.builder_args("treelet") == {"builder": "treelet"}
+    assert A.builder_args("lbvh") == {"builder": "lbvh"}
+    assert all(A.builder_args(b)["builder"] in ("lbvh", "ploc", "sah", "treelet") for b in A.BUILDERS)
