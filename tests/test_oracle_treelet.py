@@ -72,3 +72,18 @@ def test_treelet_lowers_sah_cost_on_a_mesh(oracle):
     c0 = _sah(oracle.build_bvh_treelet(v, ind, rounds=0), tri)
     c3 = _sah(oracle.build_bvh_treelet(v, ind, rounds=3), tri)
     assert c3 < 0.97 * c0
+
+
+def test_treelet_rounds_keep_trees_valid_and_never_raise_cost(oracle):
+    """Every round count the builder accepts (1..4) gives a valid tree, and a
+    further round never raises the SAH cost: a round only replaces a treelet
+    by one of least cost, and an unchanged treelet is among the candidates."""
+    pos = G.random_soup(12000, np.random.default_rng(77))
+    tri = pos.reshape(-1, 3, 3).astype(np.float32)
+    costs = []
+    for r in range(5):
+        t = oracle.build_bvh_treelet(pos, rounds=r)
+        _valid(t, tri)
+        costs.append(_sah(t, tri))
+    assert all(b <= a * (1 + 1e-6) for a, b in zip(costs, costs[1:])), costs
+    assert costs[1] < costs[0]
