@@ -1007,6 +1007,16 @@ def run_c4(ctx, torch, F, dev, pk):
     sopts = dict(persistent=2, refill_lanes=16)
     occ = b.intersectP(srays, **sopts)
     sms = _time(torch, lambda: b.intersectP(srays, out=occ, **sopts), 3, s)
+    # The plain path on the same rays: BVH2 nodes, one thread per ray (k_trace_bvh2)
+    b2 = F.RadixBVHBuilder(F.InternalTriangleMesh(pos), ctx, node_width=2)
+    b2.build()
+    hits2 = b2.intersect(rays)
+    tms2 = _time(torch, lambda: b2.intersect(rays, out=hits2), 3, s)
+    occ2 = b2.intersectP(srays)
+    sms2 = _time(torch, lambda: b2.intersectP(srays, out=occ2), 3, s)
+    same_occ = bool(torch.equal(occ2, occ))
+    del hits2, occ2
+    b2.destroy()
     # volume over the same box
     rho = F.gen_noise_grid(ctx, 512, SEED_C2 + 40)
     vol = F.DenseGridVolume(rho, medium=F.Medium(0.8, 0.2, 0.3, 0.1, 0.0), ctx=ctx)
@@ -1026,6 +1036,11 @@ def run_c4(ctx, torch, F, dev, pk):
            "build_stages_ms": {k: round(v["ms"] / 5, 4) for k, v in stages.items()},
            "primary_mrays_s": round(n / (tms * 1e-3) / 1e6, 1), "hit_rate": round(float(hit.float().mean()), 4),
            "shadow_mrays_s": round(n_sh / (sms * 1e-3) / 1e6, 1), "occluded": round(float(occ.float().mean()), 4),
+           "plain_bvh2": {"kernel": "k_trace_bvh2, one thread per ray, BVH2 nodes",
+                          "primary_mrays_s": round(n / (tms2 * 1e-3) / 1e6, 1),
+                          "shadow_mrays_s": round(n_sh / (sms2 * 1e-3) / 1e6, 1),
+                          "primary_speedup": round(tms2 / tms, 3), "shadow_speedup": round(sms2 / sms, 3),
+                          "same_occlusion": same_occ},
            "tr_fwd_ms": round(fwd, 3), "tr_adj_ms": round(adj, 3), "adj_over_fwd": round(adj / fwd, 3),
            "hit_adjoint_ms": round(hadj, 3)}
     # parity sample: 1 M camera rays and the shadow rays of their hits
